@@ -1,0 +1,144 @@
+/*
+ * lagrbf.h -- C-ABI of the GB300 implementation of LagRBF's PU-RBF interpolation and advection
+ * path (liblagrbf.so in lagrbf_gb300/).
+ *
+ * Section 1 is the drop-in surface: the same eleven exported symbols, argument meaning and
+ * error behaviour as LagRBF's ctypes interface (python_api/lagrbfpy/interface/register_cfunc.py:
+ * 50-191; implementations in src/interface/*.c).  PetscInt is int32_t, PetscReal is double,
+ * PetscInt64 is int64_t and PetscErrorCode is int (0 = success).  `is_data` is declared bool,
+ * which is how the ctypes binding passes it (register_cfunc.py:95,118).
+ *
+ * Section 2 replaces the PETSc options database that lagrbf_create() reads
+ * (LagRBFSetFromOptions, src/lagrangian_rbf.c:135-195; PUSetFromOptions,
+ * src/partition_of_unity.c:68-111; DOPRICtxSetFromOptions, src/advection/dormand_prince.c:340-353).
+ * Keys are the PETSc option names without the leading dash.
+ *
+ * Section 3 is the GPU-level extension used by the benchmark, the tests and the serving loop.
+ * It has no counterpart in the reference.
+ *
+ * Error codes follow PETSc's numbering for the analogous failures; LAGRBF_ERR_* below.
+ * No function aborts, traps or exits the process.
+ */
+#ifndef LAGRBF_GB300_H
+#define LAGRBF_GB300_H
+
+#include <stdbool.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define LAGRBF_EXPORT __attribute__((visibility("default")))
+
+enum {
+  LAGRBF_SUCCESS = 0,
+  LAGRBF_ERR_MEM = 55,            /* device or host allocation failed                     */
+  LAGRBF_ERR_SUP = 56,            /* option value not supported                            */
+  LAGRBF_ERR_ARG_SIZ = 60,        /* inconsistent sizes                                    */
+  LAGRBF_ERR_ARG_WRONG = 62,      /* e.g. a point outside the PU bounding box on fill      */
+  LAGRBF_ERR_ARG_OUTOFRANGE = 63, /* e.g. a pid outside [1, npoints] on output             */
+  LAGRBF_ERR_ARG_WRONGSTATE = 73, /* call order violated (data not filled, ...)            */
+  LAGRBF_ERR_PLIB = 77,           /* internal inconsistency                                */
+  LAGRBF_ERR_MAT_CH_ZRPVT = 81,   /* non-positive pivot in a patch Cholesky factorisation  */
+  LAGRBF_ERR_ARG_NULL = 85,       /* NULL context / array                                  */
+  LAGRBF_ERR_GPU = 97,            /* CUDA runtime error                                    */
+  LAGRBF_ERR_TIMEOUT = 200        /* a bounded device wait gave up                         */
+};
+
+/* ---------------------------------------------------------------------------------------- */
+/* 1. Drop-in surface (LagRBF ctypes interface)                                              */
+/* ---------------------------------------------------------------------------------------- */
+
+/* Replaces lagrbf_create, src/interface/interface_ctx.c:93-104 (NULL on error). */
+LAGRBF_EXPORT void *lagrbf_create(void);
+/* Replaces lagrbf_destroy, src/interface/interface_ctx.c:120-125. */
+LAGRBF_EXPORT void lagrbf_destroy(void *ctx);
+/* Replaces lagrbf_fill_swarm, src/interface/interface_utils.c:403-430.  coords is n*dim,
+   values (nullable) is n*n_interpolation_fields, pidx (nullable) holds 1-based unique ids. */
+LAGRBF_EXPORT int lagrbf_fill_swarm(void *ctx, bool is_data, int32_t npoints, double *coords, double *values,
+                                    int64_t *pidx);
+/* Replaces lagrbf_interpolation, src/interface/interface_interp.c:210-221. */
+LAGRBF_EXPORT int lagrbf_interpolation(void *ctx);
+/* Replaces lagrbf_output, src/interface/interface_utils.c:362-384.  Outputs are caller-allocated,
+   npoints rows, assembled by pid-1; rows of points no longer in the swarm are zero. */
+LAGRBF_EXPORT int lagrbf_output(void *ctx, bool is_data, int32_t npoints, double *coords, double *fields,
+                                int64_t *pidx, const char *fieldname);
+/* Replaces lagrbf_reset_coefficients, src/interface/interface_utils.c:447-458. */
+LAGRBF_EXPORT int lagrbf_reset_coefficients(void *ctx);
+/* Replaces lagrbf_avect_analytical, src/interface/interface_adv.c:75-88. */
+LAGRBF_EXPORT int lagrbf_avect_analytical(void *ctx, double time, double time_next);
+/* Replaces lagrbf_advect_interpolate, src/interface/interface_adv.c:90-106 (registered in Python
+   under the key "lagrbf_avect_interpolate"). */
+LAGRBF_EXPORT int lagrbf_advect_interpolate(void *ctx, double time, double time_next);
+/* Replaces lagrbf_advection_function, src/interface/interface_adv.c:35-53. */
+LAGRBF_EXPORT int lagrbf_advection_function(void *ctx, int (*velocity_fn)(double *, double *, void *), void *fn_ctx);
+/* Replaces lagrbf_advection_function_batch, src/interface/interface_adv.c:55-73. */
+LAGRBF_EXPORT int lagrbf_advection_function_batch(void *ctx,
+                                                  int (*velocity_fn_batch)(int32_t, int32_t, double *, double *, void *),
+                                                  void *fn_ctx);
+/* Replaces lagrbf_interpolate_driver, src/interface/interface_interp.c:167-194.  options_file
+   (nullable) uses PETSc's options-file syntax: "-key value" pairs, '#' comments. */
+LAGRBF_EXPORT void lagrbf_interpolate_driver(int32_t ndata_local, double *data_coords, double *data_values,
+                                             int32_t npoints_local, double *points_coords, double *points_values,
+                                             int32_t npoints_global, char *options_file);
+
+/* ---------------------------------------------------------------------------------------- */
+/* 2. Options store (stands in for PetscOptionsSetValue / PetscOptionsInsertFile)            */
+/* ---------------------------------------------------------------------------------------- */
+/* Keys read by lagrbf_create(): pu_mesh_dim, pu_mesh_n, pu_mesh_O, pu_mesh_L, pu_mesh_overlap,
+   pu_mesh_shape_factor, n_interpolation_fields, kernel_type, solve_method, advection,
+   advection_scheme, velocity_name, dt, cfl_fac, rmin, rmax, dopri_dt_fac, dopri_dt_fac_min,
+   dopri_dt_fac_max, dopri_atol, dopri_rtol; and the GPU-only keys eval_precision (fp64|fp32,
+   default fp64), use_cuda_graph (bool, default true).  Arrays are comma separated. */
+LAGRBF_EXPORT int lagrbf_options_set_value(const char *name, const char *value);
+LAGRBF_EXPORT int lagrbf_options_clear(void);
+LAGRBF_EXPORT int lagrbf_options_insert_file(const char *path);
+/* Copies the stored value into buf; returns 1 if found, 0 if not. */
+LAGRBF_EXPORT int lagrbf_options_get_value(const char *name, char *buf, int32_t buflen);
+
+/* ---------------------------------------------------------------------------------------- */
+/* 3. GPU-level extension (no counterpart in the reference)                                  */
+/* ---------------------------------------------------------------------------------------- */
+typedef struct {
+  int64_t launches;           /* kernels this context launched (graph nodes counted)          */
+  int64_t eval_launches;      /* launches of the PU evaluation kernel                        */
+  double  eval_flops;         /* algorithmic flops of those launches (counted on the device) */
+  double  eval_bytes;         /* algorithmic bytes of those launches                         */
+  double  eval_ms;            /* event-timed duration of those launches (profiling on)       */
+  int64_t particle_steps;     /* live particles x internal steps advanced                     */
+  int64_t steps;              /* internal time steps taken                                   */
+  int64_t patches_factored;   /* patch Cholesky factorisations performed                     */
+  double  factor_ms;          /* event-timed factorisation time (profiling on)               */
+  double  factor_flops;       /* algorithmic flops of those factorisations                   */
+  int32_t np_alive;           /* particles still in the swarm                                */
+  int32_t nd;                 /* data points in the swarm                                    */
+  int32_t max_patch;          /* largest patch (data points)                                 */
+  int32_t npatch_setup;       /* patches currently set up                                    */
+  double  dt;                 /* the advection context's current time step                   */
+} lagrbf_stats_t;
+
+/* Kernel-level event timing of the evaluation and factorisation launches (disables graph
+   capture while on, so every launch is bracketed by events on the context's stream). */
+LAGRBF_EXPORT int lagrbf_gpu_set_profiling(void *ctx, int on);
+LAGRBF_EXPORT int lagrbf_gpu_get_stats(void *ctx, lagrbf_stats_t *stats);
+LAGRBF_EXPORT int lagrbf_gpu_reset_stats(void *ctx);
+/* Blocks until all work of the context is done. */
+LAGRBF_EXPORT int lagrbf_gpu_synchronize(void *ctx);
+/* The context's cudaStream_t, as void*. */
+LAGRBF_EXPORT void *lagrbf_gpu_stream(void *ctx);
+/* Last error message of the calling thread (empty string if none). */
+LAGRBF_EXPORT const char *lagrbf_gpu_last_error(void);
+/* Per-cell/per-patch views for parity tests (host arrays sized by the caller):
+   cellid[n] of the data (is_data) or particle swarm; cell_start[ncells+1] and the data points of
+   each cell in order; patch_start[nnodes+1] and patch_pts[] (data indices, reference order). */
+LAGRBF_EXPORT int lagrbf_gpu_get_cellids(void *ctx, bool is_data, int32_t *cellid);
+LAGRBF_EXPORT int64_t lagrbf_gpu_get_patch_csr(void *ctx, int32_t *patch_start, int32_t *patch_pts);
+LAGRBF_EXPORT int64_t lagrbf_gpu_get_block_csr(void *ctx, int32_t *blk_start, int32_t *blk_pts);
+/* Geometry of the context: dim, n[3], nnodes, ncells, nen and eps_w, eps_r. */
+LAGRBF_EXPORT int lagrbf_gpu_get_geometry(void *ctx, int32_t *ints /* 7 */, double *reals /* 2 */);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,491 @@
+/*
+ * lgb_eval.cuh -- partition-of-unity RBF evaluation at particles.
+ *
+ * Replaces RBFInterpolation -> PointwiseInterpolation_{AVX512,AVX256,Scalar}
+ * (src/interpolation/interpolation.c:39-154, 178-272; interpolation_avx512.c:121-291) and the PU
+ * weights of SwarmInterpSetWeights (src/swarm/swarm_interp.c:283-396, weights_avx.c:97-243):
+ *
+ *   v_f(x_p) = sum_{k in corners(cell p)} w_k(x_p) * sum_{j in patch k} phi(|x_p - x_j|, eps_r) X_k[j, f]
+ *   w_k(x)   = phiW(|x - c_k|, eps_w) / sum_{all nodes n} phiW(|x - c_n|, eps_w)     (Wendland C2)
+ *
+ * GB300 design.  Particles are binned by cell every stage; one CTA evaluates one work unit of up to
+ * LGB_CHUNK particles of one cell.  The CTA walks the 3^dim neighbour cells of its cell in the
+ * reference's neighbour order, staging for each neighbour cell a record per data point
+ * {x, y, z, pad, X_k[j, f] for every corner patch k of the particle's cell that contains the
+ * neighbour cell} in shared memory (a fixed budget, refilled in rounds when the block does not
+ * fit).  Every thread then reads the same record (broadcast, no bank conflicts): phi is computed
+ * once per (particle, data point) and feeds the accumulators of every patch that holds the point,
+ * so the per-patch sums run in the reference's patch order (cells ascending, points ascending).
+ * Which patches a neighbour offset touches is a compile-time mask, so the accumulators stay in
+ * registers.  The PU weights need only the support nodes (<= (2*wr+2)^dim candidates): the
+ * reference's sum over all nodes adds exact zeros outside the support.
+ *
+ * Precision.  The FP64 variant follows the reference arithmetic (absolute coordinates, FP64 phi,
+ * w_k = phiW_k / sum, v += I_k * w_k).  The FP32 variant computes coordinates relative to the cell
+ * origin (so distances keep their relative precision), phi and the per-patch sums in FP32, the
+ * PU-weighted sum sum_k phiW_k * I_k with an error-free compensated accumulation (TwoSum/TwoProd
+ * into a float pair), and the weight normalisation in FP64.
+ *
+ * Roofline: FP32 (or FP64) pipe bound; per particle ~B_c*(10 + k_phi) + 2*F*sum_k m_k flops against
+ * ~(28 + 8F) bytes of particle traffic, with the block data reused by every particle of the cell.
+ */
+#pragma once
+#include <type_traits>
+#include "lgb_common.cuh"
+
+struct EvalParams {
+  lgb_geom g;
+  const int *cstart;
+  const float *xr32;      /* [nd*4] cell-relative f32 coordinates, cell order        */
+  const double *xs64;     /* [nd*dim] f64 coordinates, cell order                    */
+  const float *c32;
+  const double *c64;
+  const long long *coff;
+  const int *slot;
+  const int *setup;
+  int F, f0;
+  const int *pstart, *plist, *chunk_start;
+  const double *xp;
+  double *out;
+  int out_stride;
+  lgb_ctrl *ctrl;
+  int budget;             /* staging budget, elements of the compute type */
+};
+
+enum { KER_GENERIC = 0, KER_C2 = 1, KER_GAUSS = 2 };
+
+template <int DIM> struct EGeo {
+  static constexpr int NOFF = (DIM == 3) ? 27 : 9;
+  static constexpr int NEN = 1 << DIM;
+};
+
+__host__ __device__ constexpr int eoff_a(int o) { return o % 3 - 1; }
+__host__ __device__ constexpr int eoff_b(int o) { return (o / 3) % 3 - 1; }
+__host__ __device__ constexpr int eoff_e(int dim, int o) { return dim == 3 ? o / 9 - 1 : 0; }
+__host__ __device__ constexpr int ecorner_ox(int k) { return ((k & 3) == 1 || (k & 3) == 2) ? 1 : 0; }
+__host__ __device__ constexpr int ecorner_oy(int k) { return ((k & 3) >= 2) ? 1 : 0; }
+__host__ __device__ constexpr int ecorner_oz(int dim, int k) { return dim == 3 ? (k >> 2) : 0; }
+
+/* Corner patches of the particle's cell that contain neighbour cell `o`. */
+__host__ __device__ constexpr int einv_mask(int dim, int o)
+{
+  int m = 0;
+  for (int k = 0; k < (1 << dim); k++) {
+    int a = eoff_a(o), b = eoff_b(o), e = eoff_e(dim, o);
+    int ox = ecorner_ox(k), oy = ecorner_oy(k), oz = ecorner_oz(dim, k);
+    bool in = (a == ox - 1 || a == ox) && (b == oy - 1 || b == oy) && (dim == 2 || e == oz - 1 || e == oz);
+    if (in) m |= 1 << k;
+  }
+  return m;
+}
+__host__ __device__ constexpr int epopc(int m) { return m == 0 ? 0 : (m & 1) + epopc(m >> 1); }
+/* Slot of neighbour cell o inside the patch of corner k (ascending cell order of the patch). */
+__host__ __device__ constexpr int eslot(int dim, int k, int o)
+{
+  return (eoff_a(o) - ecorner_ox(k) + 1) + 2 * (eoff_b(o) - ecorner_oy(k) + 1) +
+         (dim == 3 ? 4 * (eoff_e(dim, o) - ecorner_oz(dim, k) + 1) : 0);
+}
+/* Record length (elements) for a neighbour offset: 4 coordinates + ninv*FP coefficients, padded
+   to a 16-byte multiple. */
+template <typename Real> __host__ __device__ constexpr int erec(int ninv, int fp)
+{
+  return sizeof(Real) == 4 ? ((4 + ninv * fp + 3) / 4) * 4 : ((4 + ninv * fp + 1) / 2) * 2;
+}
+
+template <typename Real, int KER>
+__device__ __forceinline__ Real eval_phi(Real d2, Real eps, Real ga, int kernel)
+{
+  if constexpr (sizeof(Real) == 4 && KER == KER_C2) {
+    float r = d2 * rsqrtf(fmaxf(d2, 1e-30f));
+    float u = fmaxf(1.0f - eps * r, 0.0f);
+    float u2 = u * u;
+    return (u2 * u2) * (5.0f - 4.0f * u);
+  } else if constexpr (sizeof(Real) == 4 && KER == KER_GAUSS) {
+    return exp2f(ga * d2);
+  } else {
+    return lgb_phi<Real>(kernel, sqrt(d2), eps);
+  }
+}
+
+/* Accumulate one staged segment of neighbour offset O. */
+template <typename Real, int DIM, int FP, int R, int KER, int O>
+__device__ __forceinline__ void eval_segment(const Real *__restrict__ rec, int n, const Real (&px)[R][3],
+                                             Real (&acc)[R][EGeo<DIM>::NEN][FP], Real eps, Real ga, int kernel)
+{
+  constexpr int NEN = EGeo<DIM>::NEN;
+  constexpr int MASK = einv_mask(DIM, O);
+  constexpr int NI = epopc(MASK);
+  constexpr int S = erec<Real>(NI, FP);
+  using V = typename std::conditional<sizeof(Real) == 4, float4, double2>::type;
+  constexpr int VW = sizeof(V) / sizeof(Real);
+  constexpr int NV = S / VW;
+#pragma unroll 2
+  for (int p = 0; p < n; ++p) {
+    Real v[S];
+    const V *rv = reinterpret_cast<const V *>(rec + (size_t)p * S);
+#pragma unroll
+    for (int q = 0; q < NV; q++) {
+      V t = rv[q];
+      if constexpr (VW == 4) {
+        v[4 * q + 0] = ((const float *)&t)[0]; v[4 * q + 1] = ((const float *)&t)[1];
+        v[4 * q + 2] = ((const float *)&t)[2]; v[4 * q + 3] = ((const float *)&t)[3];
+      } else {
+        v[2 * q + 0] = ((const double *)&t)[0]; v[2 * q + 1] = ((const double *)&t)[1];
+      }
+    }
+    Real phi[R];
+#pragma unroll
+    for (int r = 0; r < R; r++) {
+      Real dx = px[r][0] - v[0], dy = px[r][1] - v[1], d2;
+      if constexpr (DIM == 3) {
+        Real dz = px[r][2] - v[2];
+        d2 = fma(dx, dx, fma(dy, dy, dz * dz));
+      } else {
+        d2 = fma(dx, dx, dy * dy);
+      }
+      phi[r] = eval_phi<Real, KER>(d2, eps, ga, kernel);
+    }
+    int j = 0;
+#pragma unroll
+    for (int k = 0; k < NEN; k++) {
+      if ((MASK >> k) & 1) {
+#pragma unroll
+        for (int f = 0; f < FP; f++) {
+          Real cf = v[4 + j * FP + f];
+#pragma unroll
+          for (int r = 0; r < R; r++) acc[r][k][f] = fma(phi[r], cf, acc[r][k][f]);
+        }
+        j++;
+      }
+    }
+  }
+}
+
+template <typename Real, int DIM, int FP, int R, int KER>
+__device__ __forceinline__ void eval_dispatch(int o, const Real *rec, int n, const Real (&px)[R][3],
+                                              Real (&acc)[R][EGeo<DIM>::NEN][FP], Real eps, Real ga, int kernel)
+{
+#define EV_CASE(OO) case OO: eval_segment<Real, DIM, FP, R, KER, OO>(rec, n, px, acc, eps, ga, kernel); break;
+  if constexpr (DIM == 3) {
+    switch (o) {
+      EV_CASE(0) EV_CASE(1) EV_CASE(2) EV_CASE(3) EV_CASE(4) EV_CASE(5) EV_CASE(6) EV_CASE(7) EV_CASE(8)
+      EV_CASE(9) EV_CASE(10) EV_CASE(11) EV_CASE(12) EV_CASE(13) EV_CASE(14) EV_CASE(15) EV_CASE(16)
+      EV_CASE(17) EV_CASE(18) EV_CASE(19) EV_CASE(20) EV_CASE(21) EV_CASE(22) EV_CASE(23) EV_CASE(24)
+      EV_CASE(25) EV_CASE(26)
+      default: break;
+    }
+  } else {
+    switch (o) {
+      EV_CASE(0) EV_CASE(1) EV_CASE(2) EV_CASE(3) EV_CASE(4) EV_CASE(5) EV_CASE(6) EV_CASE(7) EV_CASE(8)
+      default: break;
+    }
+  }
+#undef EV_CASE
+}
+
+/* PU weights of one particle from the support nodes.  FP32: coordinates relative to the cell
+   origin, compensated sum.  FP64: absolute node coordinates as in the reference. */
+template <typename Real, int DIM>
+__device__ __forceinline__ void eval_weights(const lgb_geom &g, int ci, int cj, int cl, const double *x,
+                                             const Real *xr, Real (&pw)[EGeo<DIM>::NEN], double &den, int &nsupp)
+{
+  constexpr int NEN = EGeo<DIM>::NEN;
+  int cc[3] = {ci, cj, cl};
+  int lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+  /* candidate nodes: a conservative float bound of the support box (phiW is exactly zero outside
+     the support, so extra candidates change nothing) */
+  const float rad = (float)(1.0 / g.eps_w);
+  for (int d = 0; d < DIM; d++) {
+    float rel = (float)(x[d] - (g.O[d] + g.h[d] * cc[d]));
+    float ih = (float)(1.0 / g.h[d]);
+    int a = (int)floorf((rel - rad) * ih) - 1, b = (int)ceilf((rel + rad) * ih) + 1;
+    a = max(a, -cc[d]); b = min(b, g.n[d] - 1 - cc[d]);
+    lo[d] = a; hi[d] = b;
+  }
+  nsupp = 0;
+  if constexpr (sizeof(Real) == 4) {
+    float epsw = (float)g.eps_w, shi = 0.f, slo = 0.f;
+    float hf0 = (float)g.h[0], hf1 = (float)g.h[1], hf2 = (float)g.h[2];
+    for (int tz = lo[2]; tz <= hi[2]; tz++)
+      for (int ty = lo[1]; ty <= hi[1]; ty++)
+        for (int tx = lo[0]; tx <= hi[0]; tx++) {
+          float dx = xr[0] - tx * hf0, dy = xr[1] - ty * hf1, d2 = fmaf(dx, dx, dy * dy);
+          if constexpr (DIM == 3) { float dz = xr[2] - tz * hf2; d2 = fmaf(dz, dz, d2); }
+          float w = lgb_wendland_c2<float>(sqrtf(d2), epsw);
+          nsupp += (w > 0.f);
+          lgb_df_add(shi, slo, w);
+        }
+#pragma unroll
+    for (int k = 0; k < NEN; k++) {
+      float dx = xr[0] - ecorner_ox(k) * hf0, dy = xr[1] - ecorner_oy(k) * hf1, d2 = fmaf(dx, dx, dy * dy);
+      if constexpr (DIM == 3) { float dz = xr[2] - ecorner_oz(DIM, k) * hf2; d2 = fmaf(dz, dz, d2); }
+      pw[k] = lgb_wendland_c2<float>(sqrtf(d2), epsw);
+    }
+    den = (double)shi + (double)slo;
+  } else {
+    double sum = 0.0;
+    for (int tz = lo[2]; tz <= hi[2]; tz++)
+      for (int ty = lo[1]; ty <= hi[1]; ty++)
+        for (int tx = lo[0]; tx <= hi[0]; tx++) {
+          double dx = x[0] - (g.O[0] + g.h[0] * (ci + tx));
+          double dy = x[1] - (g.O[1] + g.h[1] * (cj + ty)), d2;
+          if constexpr (DIM == 3) {
+            double dz = x[2] - (g.O[2] + g.h[2] * (cl + tz));
+            d2 = fma(dx, dx, fma(dy, dy, dz * dz));
+          } else d2 = fma(dx, dx, dy * dy);
+          double w = lgb_wendland_c2<double>(sqrt(d2), g.eps_w);
+          nsupp += (w > 0.0);
+          sum += w;
+        }
+#pragma unroll
+    for (int k = 0; k < NEN; k++) {
+      double dx = x[0] - (g.O[0] + g.h[0] * (ci + ecorner_ox(k)));
+      double dy = x[1] - (g.O[1] + g.h[1] * (cj + ecorner_oy(k))), d2;
+      if constexpr (DIM == 3) {
+        double dz = x[2] - (g.O[2] + g.h[2] * (cl + ecorner_oz(DIM, k)));
+        d2 = fma(dx, dx, fma(dy, dy, dz * dz));
+      } else d2 = fma(dx, dx, dy * dy);
+      pw[k] = (Real)lgb_wendland_c2<double>(sqrt(d2), g.eps_w);
+    }
+    den = sum;
+  }
+}
+
+template <typename Real, int DIM, int FP, int R, int KER>
+__global__ void __launch_bounds__(LGB_CHUNK / R) k_eval(EvalParams P)
+{
+  constexpr int NEN = EGeo<DIM>::NEN, NOFF = EGeo<DIM>::NOFF;
+  constexpr int EVAL_T = LGB_CHUNK / R;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  Real *sm = reinterpret_cast<Real *>(smem_raw);
+  __shared__ int s_cnt[27], s_first[27], s_node[8], s_setup[8];
+  __shared__ int s_seg_o[27], s_seg_p0[27], s_seg_n[27], s_seg_base[27];
+  __shared__ int s_nseg, s_o, s_pp, s_cell, s_pbeg, s_pn, s_blk, s_wsum;
+  const lgb_geom &g = P.g;
+  const int tid = threadIdx.x;
+  const int chunk = blockIdx.x;
+  const int total = P.chunk_start[g.ncells];
+  if (chunk >= total) return;
+  if (tid == 0) {
+    int lo = 0, hi = g.ncells - 1;           /* last cell with chunk_start[c] <= chunk */
+    while (lo < hi) {
+      int mid = (lo + hi + 1) >> 1;
+      if (P.chunk_start[mid] <= chunk) lo = mid; else hi = mid - 1;
+    }
+    int c = lo;
+    int q = chunk - P.chunk_start[c];
+    int pb = P.pstart[c] + q * LGB_CHUNK;
+    s_cell = c;
+    s_pbeg = pb;
+    s_pn = min(LGB_CHUNK, P.pstart[c + 1] - pb);
+    s_wsum = 0;
+    s_o = 0;
+    s_pp = 0;
+  }
+  __syncthreads();
+  const int cell = s_cell;
+  int ci, cj, cl;
+  lgb_cell_ijk(g, cell, ci, cj, cl);
+  if (tid < NOFF) {
+    int a = eoff_a(tid), b = eoff_b(tid), e = eoff_e(DIM, tid);
+    int ni = ci + a, nj = cj + b, nl = cl + e;
+    int cnt = 0, first = 0;
+    if (ni >= 0 && ni < g.nc[0] && nj >= 0 && nj < g.nc[1] && nl >= 0 && nl < g.nc[2]) {
+      int nb = ni + nj * g.nc[0] + nl * g.nc[0] * g.nc[1];
+      first = P.cstart[nb];
+      cnt = P.cstart[nb + 1] - first;
+    }
+    s_cnt[tid] = cnt;
+    s_first[tid] = first;
+  }
+  if (tid < NEN) {
+    int node = (ci + ecorner_ox(tid)) + (cj + ecorner_oy(tid)) * g.n[0] + (cl + ecorner_oz(DIM, tid)) * g.n[0] * g.n[1];
+    s_node[tid] = node;
+    s_setup[tid] = P.setup[node];
+  }
+  __syncthreads();
+  if (tid == 0) {
+    int b = 0;
+    for (int o = 0; o < NOFF; o++) b += s_cnt[o];
+    s_blk = b;
+  }
+  __syncthreads();
+  if (s_blk == 0) return; /* empty neighbourhood: the value is left untouched (interpolation.c:89) */
+
+  /* particles of this work unit */
+  const int pn = s_pn;
+  int pid[R];
+  Real px[R][3];
+#pragma unroll
+  for (int r = 0; r < R; r++) {
+    int idx = tid + r * EVAL_T;
+    pid[r] = (idx < pn) ? P.plist[s_pbeg + idx] : -1;
+    int cc[3] = {ci, cj, cl};
+    for (int d = 0; d < 3; d++) {
+      double xv = 0.0;
+      if (d < DIM && pid[r] >= 0) xv = P.xp[(size_t)pid[r] * DIM + d];
+      if constexpr (sizeof(Real) == 4) px[r][d] = (d < DIM) ? (float)(xv - (g.O[d] + g.h[d] * cc[d])) : 0.f;
+      else px[r][d] = xv;
+    }
+  }
+  Real acc[R][NEN][FP];
+#pragma unroll
+  for (int r = 0; r < R; r++)
+#pragma unroll
+    for (int k = 0; k < NEN; k++)
+#pragma unroll
+      for (int f = 0; f < FP; f++) acc[r][k][f] = Real(0);
+
+  const Real eps = (Real)g.eps_r;
+  const Real ga = (Real)(-(g.eps_r * g.eps_r) * 1.4426950408889634);
+  const int kernel = g.kernel;
+  const Real hh[3] = {(Real)g.h[0], (Real)g.h[1], (Real)g.h[2]};
+
+  for (;;) {
+    if (tid == 0) {
+      int o = s_o, pp = s_pp, base = 0, nseg = 0;
+      while (o < NOFF) {
+        int cnt = s_cnt[o] - pp;
+        if (cnt <= 0) { o++; pp = 0; continue; }
+        int S = erec<Real>(epopc(einv_mask(DIM, o)), FP);
+        int fit = (P.budget - base) / S;
+        if (fit <= 0) break;
+        int take = min(cnt, fit);
+        s_seg_o[nseg] = o; s_seg_p0[nseg] = pp; s_seg_n[nseg] = take; s_seg_base[nseg] = base;
+        nseg++;
+        base += take * S;
+        pp += take;
+        if (pp >= s_cnt[o]) { o++; pp = 0; }
+      }
+      s_nseg = nseg; s_o = o; s_pp = pp;
+    }
+    __syncthreads();
+    const int nseg = s_nseg;
+    if (nseg == 0) break;
+    /* fill the staged records */
+    for (int sgi = 0; sgi < nseg; sgi++) {
+      const int o = s_seg_o[sgi], p0 = s_seg_p0[sgi], n = s_seg_n[sgi];
+      const int mask = einv_mask(DIM, o);
+      const int S = erec<Real>(epopc(mask), FP);
+      Real *rbase = sm + s_seg_base[sgi];
+      const int a = eoff_a(o), b = eoff_b(o), e = eoff_e(DIM, o);
+      for (int p = tid; p < n; p += EVAL_T) {
+        const int s = s_first[o] + p0 + p;
+        Real *rec = rbase + (size_t)p * S;
+        if constexpr (sizeof(Real) == 4) {
+          float4 xr = reinterpret_cast<const float4 *>(P.xr32)[s];
+          rec[0] = xr.x + a * hh[0];
+          rec[1] = xr.y + b * hh[1];
+          rec[2] = (DIM == 3) ? xr.z + e * hh[2] : 0.f;
+          rec[3] = 0.f;
+        } else {
+          rec[0] = P.xs64[(size_t)s * DIM + 0];
+          rec[1] = P.xs64[(size_t)s * DIM + 1];
+          rec[2] = (DIM == 3) ? P.xs64[(size_t)s * DIM + 2] : 0.0;
+          rec[3] = 0.0;
+        }
+        int j = 0;
+        for (int k = 0; k < NEN; k++) {
+          if (!((mask >> k) & 1)) continue;
+          const int node = s_node[k];
+          Real *dst = rec + 4 + j * FP;
+          if (s_setup[k]) {
+            long long pos = P.coff[node] + P.slot[node * 8 + eslot(DIM, k, o)] + p0 + p;
+            const size_t src = (size_t)pos * P.F + P.f0;
+            for (int f = 0; f < FP; f++) {
+              if constexpr (sizeof(Real) == 4) dst[f] = P.c32[src + f];
+              else dst[f] = P.c64[src + f];
+            }
+          } else {
+            for (int f = 0; f < FP; f++) dst[f] = Real(0);
+          }
+          j++;
+        }
+        for (int q = 4 + j * FP; q < S; q++) rec[q] = Real(0);
+      }
+    }
+    __syncthreads();
+    for (int sgi = 0; sgi < nseg; sgi++)
+      eval_dispatch<Real, DIM, FP, R, KER>(s_seg_o[sgi], sm + s_seg_base[sgi], s_seg_n[sgi], px, acc, eps, ga, kernel);
+    __syncthreads();
+  }
+
+  /* epilogue: PU weights and the weighted sum */
+  int wloc = 0;
+#pragma unroll
+  for (int r = 0; r < R; r++) {
+    if (pid[r] < 0) continue;
+    Real pw[NEN];
+    double den;
+    int ns;
+    double xabs[3];
+    for (int d = 0; d < 3; d++) xabs[d] = (d < DIM) ? P.xp[(size_t)pid[r] * DIM + d] : 0.0;
+    eval_weights<Real, DIM>(g, ci, cj, cl, xabs, px[r], pw, den, ns);
+    wloc += ns;
+    double *o = P.out + (size_t)pid[r] * P.out_stride;
+    if constexpr (sizeof(Real) == 4) {
+      double inv = (den > 0.0) ? 1.0 / den : 0.0;
+#pragma unroll
+      for (int f = 0; f < FP; f++) {
+        float hi = 0.f, lo = 0.f;
+#pragma unroll
+        for (int k = 0; k < NEN; k++) {
+          float prod = pw[k] * acc[r][k][f];
+          float perr = fmaf(pw[k], acc[r][k][f], -prod);
+          lgb_df_add(hi, lo, prod);
+          lo += perr;
+        }
+        o[f] = ((double)hi + (double)lo) * inv;
+      }
+    } else {
+      double val[FP];
+#pragma unroll
+      for (int f = 0; f < FP; f++) val[f] = 0.0;
+#pragma unroll
+      for (int k = 0; k < NEN; k++) {
+        double w = (den > 0.0) ? (double)pw[k] / den : 0.0;
+#pragma unroll
+        for (int f = 0; f < FP; f++) val[f] += (double)acc[r][k][f] * w;
+      }
+#pragma unroll
+      for (int f = 0; f < FP; f++) o[f] = val[f];
+    }
+  }
+  /* algorithmic work of this unit (SURVEY-style count: distances 10, kernel k_phi, 2 flops per
+     coefficient FMA, 18 per support node of the weights, 2F+1 per corner in the epilogue) */
+  for (int off = 16; off > 0; off >>= 1) wloc += __shfl_down_sync(0xffffffffu, wloc, off);
+  if ((tid & 31) == 0) atomicAdd(&s_wsum, wloc);
+  __syncthreads();
+  if (tid == 0) {
+    long long msum = 0;
+    for (int o = 0; o < NOFF; o++) {
+      int mask = einv_mask(DIM, o), ninv = 0;
+      for (int k = 0; k < NEN; k++) ninv += ((mask >> k) & 1) && s_setup[k];
+      msum += (long long)s_cnt[o] * ninv;
+    }
+    double kphi = (KER == KER_GAUSS || g.kernel == LGB_KERNEL_GAUSSIAN) ? 4.0 : 8.0;
+    double fl = (double)pn * ((double)s_blk * (10.0 + kphi) + 2.0 * FP * (double)msum + NEN * (2.0 * FP + 1.0)) +
+                18.0 * (double)s_wsum;
+    double by = (double)pn * (8.0 * DIM + 4.0 + 8.0 * FP) +
+                (double)s_blk * (sizeof(Real) == 4 ? 16.0 : 8.0 * DIM) + (double)msum * FP * sizeof(Real);
+    atomicAdd(&P.ctrl->eval_flops, fl);
+    atomicAdd(&P.ctrl->eval_bytes, by);
+  }
+}
+
+/* FP64 PU weights of every live particle (output of the "weights" field). */
+template <int DIM>
+__global__ void k_weights(lgb_geom g, int np, const double *__restrict__ xp, const int *__restrict__ cell,
+                          const int *__restrict__ alive, double *__restrict__ w)
+{
+  constexpr int NEN = EGeo<DIM>::NEN;
+  int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= np || !alive[p] || cell[p] < 0) return;
+  int ci, cj, cl;
+  lgb_cell_ijk(g, cell[p], ci, cj, cl);
+  double x[3] = {xp[(size_t)p * DIM], xp[(size_t)p * DIM + 1], DIM == 3 ? xp[(size_t)p * DIM + 2] : 0.0};
+  double pw[NEN], den;
+  int ns;
+  eval_weights<double, DIM>(g, ci, cj, cl, x, x, pw, den, ns);
+  for (int k = 0; k < NEN; k++) w[(size_t)p * NEN + k] = (den > 0.0) ? pw[k] / den : 0.0;
+}

@@ -1,0 +1,141 @@
+/*
+ * lgb_internal.h -- state shared by the C host layer (lgb_host.c) and the CUDA operations
+ * (lgb_bin.cu, lgb_eval.cu, lgb_factor.cu, lgb_step.cu).  Plain C: device memory appears as
+ * typed pointers, streams as void*.
+ *
+ * HBM layout of one context (all arrays device-resident for the lifetime of the dataset):
+ *   data swarm      xd[nd*dim] f64 (fill order), fd[nd*F] f64,
+ *                   cell_d[nd], cstart[ncells+1], sorted[nd] (fill index of the s-th point in
+ *                   cell order), xs[nd*dim] f64 and xr[nd*4] f32 (cell order; xr is relative to
+ *                   the point's own cell origin), fs[nd*F] f64 (cell order)
+ *   patches         pm[nnodes] sizes, slot[nnodes*8] offset of each adjacent cell inside the
+ *                   patch, coff[nnodes+1] i64 pool offsets (points), c64/c32 coefficient pools
+ *                   [sum_k m_k * F] laid out [patch][point][field], foff/fac packed lower
+ *                   Cholesky factors (only when factors are kept), setup/solved flags
+ *   particle swarm  xp[np*dim], fields[np*F], vel[np*dim], x0[np*dim], vadv[7][np*dim] f64,
+ *                   cell_p[np], alive[np]; per-stage binning pcount/pstart[ncells+1],
+ *                   pfill[ncells], plist[np], chunk_start[ncells+1]
+ */
+#ifndef LGB_INTERNAL_H
+#define LGB_INTERNAL_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum { LGB_KERNEL_LINEAR = 0, LGB_KERNEL_WENDLAND_C0, LGB_KERNEL_WENDLAND_C2, LGB_KERNEL_BUMP,
+       LGB_KERNEL_MQ, LGB_KERNEL_IMQ, LGB_KERNEL_GAUSSIAN };
+enum { LGB_RK1 = 0, LGB_RK2 = 1, LGB_RK4 = 2, LGB_DOPRI = 3 };
+enum { LGB_A_FACTOR = 0, LGB_A_KSP = 1, LGB_A_KSP_ASMB = 2 };
+enum { LGB_PREC_FP64 = 0, LGB_PREC_FP32 = 1 };
+
+/* Particles per evaluation work unit (one CTA): 128 threads x 2 particles. */
+#define LGB_CHUNK 256
+
+/* PU mesh geometry (DMDA with Q1 elements): nodes are patches, elements are cells. */
+typedef struct {
+  int dim, nen, kernel;
+  int n[3];        /* nodes per axis (1 beyond dim)                      */
+  int nc[3];       /* cells per axis (1 beyond dim)                      */
+  int nnodes, ncells;
+  int wr;          /* weight-support half width in node spacings          */
+  double O[3], L[3], h[3];
+  double eps_w, eps_r;
+} lgb_geom;
+
+/* Device-resident control block of the advection loop: the scalars of
+   InternalForwardAdvectionLoop (time_loop.c:39-100) and of the schemes that kernels read. */
+typedef struct {
+  double t, t_next;
+  double dt;           /* step of the current internal step                          */
+  double dt_adv;       /* advection context dt (DOPRI stores its adapted step here)   */
+  double cfl_fac, cfl_radius;
+  double dopri_fac, dopri_fac_min, dopri_fac_max, dopri_atol, dopri_rtol;
+  double rmin, rmax;
+  double dopri_error;
+  unsigned long long dtcfl_bits;  /* atomicMin target (bits of a positive double)     */
+  unsigned long long maxerr_bits; /* atomicMax target (bits of a non-negative double) */
+  int any_alive;
+  int scheme;
+  int steps;
+  int np_alive;
+  long long particle_steps;
+  double eval_flops;   /* accumulated algorithmic flops of evaluation launches   */
+  double eval_bytes;   /* accumulated algorithmic bytes of evaluation launches   */
+  int nwork;           /* patches queued for set-up / solve                       */
+  int factor_error;    /* first non-positive pivot row (1-based), 0 if none        */
+  int factor_node;     /* patch with that pivot                                    */
+  int nfactored;
+  double factor_flops;
+} lgb_ctrl;
+
+typedef struct {
+  lgb_geom g;
+  int F;               /* n_interpolation_fields */
+  int prec;            /* LGB_PREC_*             */
+  int solve_method;
+  int keep_factors;
+  /* data swarm */
+  int nd, nd_cap;
+  double *xd, *fd, *xs, *fs;
+  float *xr;
+  int *cell_d, *cstart, *sorted, *dfill, *dtmp;
+  int max_cell_pts;
+  /* patches */
+  int *pm, *slot, *setup, *solved, *work, *status;
+  int *need;          /* 2*nnodes ints: flags, also borrowed as nnodes int64 scratch */
+  long long *coff, *foff;
+  long long coef_cap, fac_cap;
+  double *c64, *fac;
+  float *c32;
+  int max_patch;
+  double *ws;          /* factorisation workspace: nws slots of ws_stride doubles */
+  long long ws_stride;
+  int nws;
+  /* particle swarm */
+  int np, np_cap;
+  double *xp, *fields, *vel, *x0, *vadv;
+  int *cell_p, *alive, *pcount, *pstart, *pfill, *plist, *chunk_start;
+  int max_chunks;
+  /* scratch for scans */
+  int *scan_tmp;
+  long long *scan_tmp64;
+  /* control */
+  lgb_ctrl *ctrl;
+  int smem_optin;      /* cudaDevAttrMaxSharedMemoryPerBlockOptin */
+  int nsm;
+} lgb_dev;
+
+/* ---- operations implemented in CUDA (each returns a cudaError_t as int, 0 = success) ---- */
+/* lgb_bin.cu */
+int lgb_op_locate(const lgb_geom *g, int n, const double *x, int *cell, int *alive, int *counts, int *nbad,
+                  void *stream);
+int lgb_op_scan_i32(int n, const int *in, int *out, int *tmp, void *stream);
+int lgb_op_scan_i64(int n, const long long *in, long long *out, long long *tmp, void *stream);
+int lgb_op_scatter(int n, const int *cell, const int *alive, const int *start, int *fill, int *list, void *stream);
+int lgb_op_data_arrange(lgb_dev *d, void *stream);      /* xs, xr, fs, patch sizes, slots, offsets */
+int lgb_op_data_values(lgb_dev *d, void *stream);       /* fs only (values changed)                */
+int lgb_op_bin_particles(lgb_dev *d, int mark_dead, void *stream); /* cell_p, pcount, pstart, plist, chunks */
+int lgb_op_mark_patches(lgb_dev *d, void *stream);      /* queue patches touched by live particles */
+/* lgb_factor.cu */
+int lgb_op_factor(lgb_dev *d, void *stream);            /* set up / solve queued patches */
+/* lgb_eval.cu */
+int lgb_op_eval(lgb_dev *d, int nf_first, int nf, double *out, int out_stride, void *stream);
+int lgb_op_weights(lgb_dev *d, double *w, void *stream);
+/* lgb_step.cu */
+int lgb_op_stage(lgb_dev *d, int scheme, int stage, void *stream);
+int lgb_op_dopri_error(lgb_dev *d, void *stream);
+int lgb_op_ctrl(lgb_dev *d, int what, void *stream);
+enum { LGB_CTRL_BEGIN_STEP = 0, LGB_CTRL_END_STEP = 1, LGB_CTRL_RESET_CFL = 2, LGB_CTRL_DOPRI_DT = 3 };
+int lgb_op_copy_velocity(lgb_dev *d, void *stream);     /* vel <- fields[:, :dim] */
+int lgb_op_count_alive(lgb_dev *d, void *stream);
+int lgb_device_info(int *nsm, int *smem_optin);
+long long lgb_launch_count(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

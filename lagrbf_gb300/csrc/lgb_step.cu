@@ -1,0 +1,259 @@
+/*
+ * lgb_step.cu -- explicit advection stages and the device-side step control.
+ *
+ * Replaces AdvectionExplicit_Scalar (src/advection/advection.c:36-57), the stage drivers of
+ * runge_kutta_1.c:37-75, runge_kutta_2.c:38-91, runge_kutta_4.c:45-156 and dormand_prince.c:
+ * 37-310, AdvectionComputeTimestep_CFL (advection.c:430-470), AdvectionCopyVelocityField
+ * (advection.c:298-316) and the loop scalars of InternalForwardAdvectionLoop (time_loop.c:39-100).
+ *
+ * Every stage is one pass over the particles that writes the stage position (and commits the
+ * previous stage velocity into v_adv), followed by re-binning and one evaluation.  The global
+ * reductions of the reference (CFL min dt, DOPRI max error: MPI_Allreduce sites advection.c:466,
+ * dormand_prince.c:93) are warp-reduced atomics on the ordered bit patterns of non-negative
+ * doubles.  The loop scalars (t, dt, DOPRI dt) live in a device control block, so a whole
+ * internal step is a fixed sequence of launches that the host captures once in a CUDA graph.
+ */
+#include "lgb_common.cuh"
+#include <float.h>
+
+__constant__ double c_dp_a[6][6] = {
+  {1.0 / 5.0, 0, 0, 0, 0, 0},
+  {3.0 / 40.0, 9.0 / 40.0, 0, 0, 0, 0},
+  {44.0 / 45.0, -56.0 / 15.0, 32.0 / 9.0, 0, 0, 0},
+  {19372.0 / 6561.0, -25360.0 / 2187.0, 64448.0 / 6561.0, -212.0 / 729.0, 0, 0},
+  {9017.0 / 3168.0, -355.0 / 33.0, 46732.0 / 5247.0, 49.0 / 176.0, -5103.0 / 18656.0, 0},
+  {35.0 / 384.0, 0, 500.0 / 1113.0, 125.0 / 192.0, -2187.0 / 6784.0, 11.0 / 84.0}};
+__constant__ double c_dp_e[7] = {5179.0 / 57600.0, 0, 7571.0 / 16695.0, 393.0 / 640.0, -92097.0 / 339200.0,
+                                 187.0 / 2100.0, 1.0 / 40.0};
+
+/* AdvectionProjectOntoSphereBoundary_Pointwise (advection.c:472-491) */
+__device__ __forceinline__ void project_sphere(double *x, int dim, double rmin, double rmax)
+{
+  double pos = 0.0, normal[3];
+  for (int d = 0; d < dim; d++) pos += x[d] * x[d];
+  if (pos < rmax * rmax && pos > rmin * rmin) return;
+  pos = sqrt(pos);
+  for (int d = 0; d < dim; d++) normal[d] = x[d] / pos;
+  if (pos > rmax) for (int d = 0; d < dim; d++) x[d] = rmax * normal[d];
+  else for (int d = 0; d < dim; d++) x[d] = rmin * normal[d];
+}
+
+struct StageParams {
+  int np, dim, scheme, stage;
+  double *xp, *x0, *vel, *vadv;
+  const int *alive;
+  const lgb_ctrl *ctrl;
+};
+
+__global__ void k_stage(StageParams S)
+{
+  int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= S.np || !S.alive[p]) return;
+  const int dim = S.dim;
+  const double dt = S.ctrl->dt;
+  const double rmin = S.ctrl->rmin, rmax = S.ctrl->rmax;
+  const size_t o = (size_t)p * dim;
+  const size_t st = (size_t)S.np * dim; /* stride between v_adv stages */
+  double x[3], x0[3], v[3];
+  for (int d = 0; d < dim; d++) { x[d] = S.xp[o + d]; v[d] = S.vel[o + d]; }
+  switch (S.scheme) {
+  case LGB_RK1:
+    /* runge_kutta_1.c:61-64: x = x0 + dt * v */
+    for (int d = 0; d < dim; d++) S.xp[o + d] = x[d] + dt * v[d];
+    return;
+  case LGB_RK2:
+    if (S.stage == 0) {
+      for (int d = 0; d < dim; d++) { S.x0[o + d] = x[d]; S.xp[o + d] = x[d] + (0.5 * dt) * v[d]; }
+    } else {
+      for (int d = 0; d < dim; d++) S.xp[o + d] = S.x0[o + d] + dt * v[d];
+    }
+    return;
+  case LGB_RK4: {
+    const double c[3] = {0.5, 0.5, 1.0};
+    if (S.stage == 0) for (int d = 0; d < dim; d++) x0[d] = x[d];
+    else for (int d = 0; d < dim; d++) x0[d] = S.x0[o + d];
+    /* commit v_adv_{stage} = velocity (stage 0: AdvectionSetInitialValues) */
+    for (int d = 0; d < dim; d++) S.vadv[S.stage * st + o + d] = v[d];
+    if (S.stage == 0) for (int d = 0; d < dim; d++) S.x0[o + d] = x0[d];
+    if (S.stage < 3) {
+      double xs[3];
+      for (int d = 0; d < dim; d++) xs[d] = x0[d] + (c[S.stage] * dt) * v[d];
+      project_sphere(xs, dim, rmin, rmax);
+      for (int d = 0; d < dim; d++) S.xp[o + d] = xs[d];
+    } else {
+      const double w[4] = {1.0, 2.0, 2.0, 1.0};
+      double xs[3];
+      for (int d = 0; d < dim; d++) xs[d] = x[d]; /* components not yet updated keep the stage-3 value */
+      for (int d = 0; d < dim; d++) {
+        double sum = 0.0;
+        for (int s = 0; s < 4; s++) sum += w[s] * S.vadv[s * st + o + d];
+        xs[d] = x0[d] + dt / 6.0 * sum;
+        project_sphere(xs, dim, rmin, rmax); /* runge_kutta_4.c:140, inside the component loop */
+      }
+      for (int d = 0; d < dim; d++) S.xp[o + d] = xs[d];
+    }
+    return;
+  }
+  case LGB_DOPRI: {
+    const int s = S.stage; /* 0..5 */
+    if (s == 0) for (int d = 0; d < dim; d++) { x0[d] = x[d]; S.x0[o + d] = x[d]; }
+    else for (int d = 0; d < dim; d++) x0[d] = S.x0[o + d];
+    for (int d = 0; d < dim; d++) S.vadv[s * st + o + d] = v[d];
+    double vs[3] = {0.0, 0.0, 0.0}, xs[3];
+    for (int j = 0; j <= s; j++)
+      for (int d = 0; d < dim; d++) {
+        double vj = (j == s) ? v[d] : S.vadv[j * st + o + d];
+        vs[d] += c_dp_a[s][j] * vj;
+      }
+    for (int d = 0; d < dim; d++) { S.vel[o + d] = vs[d]; xs[d] = x0[d] + dt * vs[d]; }
+    project_sphere(xs, dim, rmin, rmax);
+    for (int d = 0; d < dim; d++) S.xp[o + d] = xs[d];
+    return;
+  }
+  default: return;
+  }
+}
+
+extern "C" int lgb_op_stage(lgb_dev *d, int scheme, int stage, void *stream)
+{
+  if (d->np <= 0) return 0;
+  StageParams S;
+  S.np = d->np; S.dim = d->g.dim; S.scheme = scheme; S.stage = stage;
+  S.xp = d->xp; S.x0 = d->x0; S.vel = d->vel; S.vadv = d->vadv; S.alive = d->alive; S.ctrl = d->ctrl;
+  k_stage<<<lgb_cdiv(d->np, 256), 256, 0, (cudaStream_t)stream>>>(S);
+  lgb_count_launch(1);
+  return (int)cudaGetLastError();
+}
+
+/* DOPRI embedded error (dormand_prince.c:37-102): commits v_adv_6, per-particle error norm,
+   global max. */
+__global__ void k_dopri_error(int np, int dim, const double *__restrict__ xp, const double *__restrict__ x0,
+                              const double *__restrict__ vel, double *__restrict__ vadv,
+                              const int *__restrict__ alive, lgb_ctrl *ctrl)
+{
+  int p = blockIdx.x * blockDim.x + threadIdx.x;
+  double E = -1.0;
+  if (p < np && alive[p]) {
+    const size_t o = (size_t)p * dim, st = (size_t)np * dim;
+    const double dt = ctrl->dt, atol = ctrl->dopri_atol, rtol = ctrl->dopri_rtol;
+    for (int d = 0; d < dim; d++) vadv[6 * st + o + d] = vel[o + d];
+    double vlow[3] = {0.0, 0.0, 0.0};
+    for (int i = 0; i < 7; i++)
+      for (int d = 0; d < dim; d++) vlow[d] += c_dp_e[i] * vadv[i * st + o + d];
+    double e2 = 0.0;
+    for (int d = 0; d < dim; d++) {
+      double xa = x0[o + d], xb = xp[o + d];
+      double mv = (fabs(xa) < fabs(xb)) ? fabs(xb) : fabs(xa);
+      double tol = atol + rtol * mv;
+      double err = xb - (xa + dt * vlow[d]);
+      e2 += (err * err) / (tol * tol);
+    }
+    E = sqrt(1.0 / dim * e2);
+  }
+  /* warp max then one atomic per warp (E >= 0 orders like its bit pattern) */
+  for (int off = 16; off > 0; off >>= 1) E = fmax(E, __shfl_down_sync(0xffffffffu, E, off));
+  if ((threadIdx.x & 31) == 0 && E >= 0.0) {
+    atomicMax(&ctrl->maxerr_bits, (unsigned long long)__double_as_longlong(E));
+    ctrl->any_alive = 1;
+  }
+}
+
+extern "C" int lgb_op_dopri_error(lgb_dev *d, void *stream)
+{
+  if (d->np <= 0) return 0;
+  k_dopri_error<<<lgb_cdiv(d->np, 256), 256, 0, (cudaStream_t)stream>>>(d->np, d->g.dim, d->xp, d->x0, d->vel,
+                                                                          d->vadv, d->alive, d->ctrl);
+  lgb_count_launch(1);
+  return (int)cudaGetLastError();
+}
+
+/* velocity <- fields[:, :dim] (when copy), then CFL dt = min cfl*radius/(|v| + 1e-16) and the
+   number of live particles. */
+__global__ void k_velocity_cfl(int np, int dim, int F, int copy, const double *__restrict__ fields,
+                               double *__restrict__ vel, const int *__restrict__ alive, lgb_ctrl *ctrl)
+{
+  int p = blockIdx.x * blockDim.x + threadIdx.x;
+  double dtl = DBL_MAX;
+  int live = 0;
+  if (p < np && alive[p]) {
+    live = 1;
+    double n2 = 0.0;
+    for (int d = 0; d < dim; d++) {
+      double v = copy ? ((d < F) ? fields[(size_t)p * F + d] : 0.0) : vel[(size_t)p * dim + d];
+      if (copy) vel[(size_t)p * dim + d] = v;
+      n2 += v * v;
+    }
+    dtl = ctrl->cfl_fac * ctrl->cfl_radius / (sqrt(n2) + 1e-16);
+  }
+  for (int off = 16; off > 0; off >>= 1) {
+    dtl = fmin(dtl, __shfl_down_sync(0xffffffffu, dtl, off));
+    live += __shfl_down_sync(0xffffffffu, live, off);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    if (dtl < DBL_MAX) atomicMin(&ctrl->dtcfl_bits, (unsigned long long)__double_as_longlong(dtl));
+    if (live) atomicAdd(&ctrl->np_alive, live);
+  }
+}
+
+extern "C" int lgb_op_copy_velocity(lgb_dev *d, void *stream)
+{
+  if (d->np <= 0) return 0;
+  k_velocity_cfl<<<lgb_cdiv(d->np, 256), 256, 0, (cudaStream_t)stream>>>(d->np, d->g.dim, d->F, 1, d->fields,
+                                                                           d->vel, d->alive, d->ctrl);
+  lgb_count_launch(1);
+  return (int)cudaGetLastError();
+}
+
+extern "C" int lgb_op_count_alive(lgb_dev *d, void *stream)
+{
+  if (d->np <= 0) return 0;
+  k_velocity_cfl<<<lgb_cdiv(d->np, 256), 256, 0, (cudaStream_t)stream>>>(d->np, d->g.dim, d->F, 0, d->fields,
+                                                                           d->vel, d->alive, d->ctrl);
+  lgb_count_launch(1);
+  return (int)cudaGetLastError();
+}
+
+/* Loop scalars of InternalForwardAdvectionLoop, one thread. */
+__global__ void k_ctrl(lgb_ctrl *c, int what)
+{
+  switch (what) {
+  case LGB_CTRL_RESET_CFL:
+    c->dtcfl_bits = (unsigned long long)__double_as_longlong(DBL_MAX);
+    c->np_alive = 0;
+    break;
+  case LGB_CTRL_BEGIN_STEP: {
+    double dt_cfl = __longlong_as_double((long long)c->dtcfl_bits);
+    double dt = (c->scheme == LGB_DOPRI) ? ((c->dt_adv < dt_cfl) ? c->dt_adv : dt_cfl) : dt_cfl;
+    if (c->t + dt > c->t_next) dt = c->t_next - c->t;
+    c->dt = dt;
+    c->dt_adv = dt; /* LagRBFSetTimeStep */
+    c->maxerr_bits = 0ull;
+    c->any_alive = 0;
+    break;
+  }
+  case LGB_CTRL_DOPRI_DT: {
+    /* AdvectionComputeAdaptiveTimeStep_DOPRI (dormand_prince.c:179-214) */
+    double max_err = c->any_alive ? __longlong_as_double((long long)c->maxerr_bits) : -DBL_MAX;
+    double fac_max = (max_err <= 1.0) ? c->dopri_fac_max : 1.0;
+    double q = c->dopri_fac * pow(1.0 / max_err, 1.0 / 5.0);
+    double inner = (c->dopri_fac_min < q) ? q : c->dopri_fac_min; /* PetscMax */
+    double f = (fac_max < inner) ? fac_max : inner;               /* PetscMin */
+    c->dopri_error = max_err;
+    c->dt_adv = c->dt * f;
+    break;
+  }
+  case LGB_CTRL_END_STEP:
+    c->t += c->dt;
+    c->steps += 1;
+    c->particle_steps += c->np_alive;
+    break;
+  default: break;
+  }
+}
+
+extern "C" int lgb_op_ctrl(lgb_dev *d, int what, void *stream)
+{
+  k_ctrl<<<1, 1, 0, (cudaStream_t)stream>>>(d->ctrl, what);
+  lgb_count_launch(1);
+  return (int)cudaGetLastError();
+}

@@ -1,0 +1,1169 @@
+/*
+ * lagrbf_oracle.c -- CPU restatement of LagRBF's PU-RBF interpolation and advection path.
+ *
+ * TEST INFRASTRUCTURE ONLY (parity checker, CPU baseline).  See lagrbf_oracle.h for the
+ * parity status and the conventions fixed where the reference delegates to PETSc.
+ *
+ * Build without fast-math and with -ffp-contract=off so that every fma() below is the only
+ * fused operation: the association of sums follows the reference's vector code (8-lane chunks
+ * in interpolation_avx512.c, 4-lane chunks in weights_avx.c) and stays identical on x86-64 and
+ * aarch64.
+ */
+#include "lagrbf_oracle.h"
+
+#include <math.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include <float.h>
+#include <time.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#define ORC_MAX_REAL DBL_MAX
+#define ORC_MIN(a, b) (((a) < (b)) ? (a) : (b)) /* PetscMin */
+#define ORC_MAX(a, b) (((a) < (b)) ? (b) : (a)) /* PetscMax */
+
+/* Error codes follow PETSc's numbering for the analogous failures. */
+#define ORC_ERR_ARG_SIZ 60
+#define ORC_ERR_ARG_WRONG 62
+#define ORC_ERR_ARG_OUTOFRANGE 63
+#define ORC_ERR_ARG_WRONGSTATE 73
+#define ORC_ERR_PLIB 77
+#define ORC_ERR_MAT_CH_ZRPVT 81
+#define ORC_ERR_ARG_NULL 85
+#define ORC_ERR_MEM 55
+#define ORC_ERR_SUP 56
+
+/* ======================================================================================= */
+/* configuration                                                                            */
+/* ======================================================================================= */
+void orc_config_default(orc_config *cfg)
+{
+  memset(cfg, 0, sizeof(*cfg));
+  cfg->dim = 3;
+  cfg->n[0] = cfg->n[1] = cfg->n[2] = 4;
+  cfg->O[0] = cfg->O[1] = cfg->O[2] = 0.0;
+  cfg->L[0] = cfg->L[1] = cfg->L[2] = 1.0;
+  cfg->overlap = 1.0;                 /* partition_of_unity.c:103 */
+  cfg->shape_factor = 1.0;            /* partition_of_unity.c:58 */
+  cfg->kernel = ORC_KERNEL_LINEAR;    /* lagrangian_rbf.c:47 */
+  cfg->solve_method = ORC_A_FACTOR;   /* lagrangian_rbf.c:63 */
+  cfg->nfields = 0;
+  cfg->advection = 0;
+  cfg->scheme = ORC_DOPRI;            /* lagrangian_rbf.c:186 */
+  cfg->cfl_fac = 0.4;                 /* lagrangian_rbf.c:58 */
+  cfg->dt = 1e-10;                    /* advection_ctx.c:62 */
+  cfg->rmin = 0.0;
+  cfg->rmax = ORC_MAX_REAL;
+  cfg->dopri_dt_fac = 0.9;            /* dormand_prince.c:318-322 */
+  cfg->dopri_dt_fac_min = 1.0e-2;
+  cfg->dopri_dt_fac_max = 1.0e2;
+  cfg->dopri_atol = 1.0e-3;
+  cfg->dopri_rtol = 1.0e-3;
+}
+
+/* ======================================================================================= */
+/* geometry                                                                                 */
+/* ======================================================================================= */
+void orc_pu_setup(orc_pu *pu, const orc_config *cfg)
+{
+  int d;
+  double box_length = 0.0, overlap, radius;
+  memset(pu, 0, sizeof(*pu));
+  pu->dim = cfg->dim;
+  pu->nnodes = 1;
+  pu->ncells = 1;
+  for (d = 0; d < 3; d++) {
+    if (d < cfg->dim) {
+      pu->n[d] = cfg->n[d];
+      pu->O[d] = cfg->O[d];
+      pu->L[d] = cfg->L[d];
+      pu->h[d] = (pu->L[d] - pu->O[d]) / (double)(pu->n[d] - 1); /* DMDASetUniformCoordinates */
+    } else {
+      pu->n[d] = 1; pu->O[d] = 0.0; pu->L[d] = 0.0; pu->h[d] = 1.0;
+    }
+  }
+  for (d = 0; d < cfg->dim; d++) { pu->nnodes *= pu->n[d]; pu->ncells *= (pu->n[d] - 1); }
+  pu->nen = 1 << cfg->dim;
+  /* PartitionOfUnityComputeSupport, partition_of_unity.c:322-346 */
+  for (d = 0; d < cfg->dim; d++) box_length = ORC_MAX(box_length, (pu->L[d] - pu->O[d]));
+  overlap = cfg->overlap * box_length;
+  radius = overlap / pow((double)pu->nnodes, 1.0 / cfg->dim);
+  pu->eps_w = 1.0 / radius;
+  /* PartitionOfUnityComputeShapeFactor, partition_of_unity.c:348-355 */
+  pu->eps_r = cfg->shape_factor * pu->eps_w;
+}
+
+static inline double node_coord(const orc_pu *pu, int d, int i) { return pu->O[d] + pu->h[d] * i; }
+
+int orc_cell_corner(const orc_pu *pu, int cell, int k)
+{
+  /* PETSc Q1 element node order: counter-clockwise on the lower face, then the upper face. */
+  static const int off2[4][2] = {{0, 0}, {1, 0}, {1, 1}, {0, 1}};
+  static const int off3[8][3] = {{0, 0, 0}, {1, 0, 0}, {1, 1, 0}, {0, 1, 0},
+                                 {0, 0, 1}, {1, 0, 1}, {1, 1, 1}, {0, 1, 1}};
+  int cx = pu->n[0] - 1, cy = pu->n[1] - 1;
+  int i, j, l;
+  if (pu->dim == 2) {
+    j = cell / cx; i = cell - j * cx;
+    return (i + off2[k][0]) + (j + off2[k][1]) * pu->n[0];
+  }
+  l = cell / (cx * cy); j = (cell - l * cx * cy) / cx; i = cell - l * cx * cy - j * cx;
+  return (i + off3[k][0]) + (j + off3[k][1]) * pu->n[0] + (l + off3[k][2]) * pu->n[0] * pu->n[1];
+}
+
+/* ======================================================================================= */
+/* RBF kernels, kernels_rbf.c:31-91 (scalar) and kernels_rbf_avx512.h / _avx.h (lane form)  */
+/* ======================================================================================= */
+double orc_phi_scalar(int kernel, double r, double eps)
+{
+  double u;
+  switch (kernel) {
+  case ORC_KERNEL_LINEAR: return eps * r;
+  case ORC_KERNEL_WENDLAND_C0: u = 1.0 - eps * r; if (u < 0.0) return 0.0; return u * u;
+  case ORC_KERNEL_WENDLAND_C2: u = 1.0 - eps * r; if (u < 0.0) return 0.0; return pow(u, 4) * (5.0 - 4.0 * u);
+  case ORC_KERNEL_BUMP: u = 1.0 - eps * r; if (u < 0.0) return 0.0; return exp(-1.0 / (u * (2.0 - u)));
+  case ORC_KERNEL_MQ: u = eps * r; return sqrt(1.0 + u * u);
+  case ORC_KERNEL_IMQ: u = eps * r; return 1.0 / sqrt(1.0 + u * u);
+  case ORC_KERNEL_GAUSSIAN: u = eps * r; return exp(-u * u);
+  default: return NAN;
+  }
+}
+
+/* One lane of the vector kernels (same operation order as the intrinsics).  The reference's
+   vector exp (exp_avx.h) is a polynomial approximation; libm exp stands in for it, so the
+   Gaussian and bump kernels agree with the reference to about one ulp, not bit for bit. */
+static inline double phi_lane(int kernel, double r, double eps)
+{
+  double u, u2, u4, inner;
+  switch (kernel) {
+  case ORC_KERNEL_LINEAR: return eps * r;
+  case ORC_KERNEL_WENDLAND_C0: u = 1.0 - eps * r; if (!(u >= 0.0)) u = 0.0; return u * u;
+  case ORC_KERNEL_WENDLAND_C2:
+    u = 1.0 - eps * r;
+    if (!(u >= 0.0)) return 0.0;
+    u2 = u * u; u4 = u2 * u2; inner = 5.0 - 4.0 * u;
+    return u4 * inner;
+  case ORC_KERNEL_BUMP:
+    u = 1.0 - eps * r;
+    if (!(u >= 0.0)) return 0.0;
+    return exp(-1.0 / (u * (2.0 - u)));
+  case ORC_KERNEL_GAUSSIAN: u = eps * r; u2 = u * u; return exp(u2 * -1.0);
+  default: return orc_phi_scalar(kernel, r, eps); /* MQ / IMQ have no vector form */
+  }
+}
+
+/* ======================================================================================= */
+/* binning                                                                                  */
+/* ======================================================================================= */
+/* Convention (PETSc DMLocatePoints on the uniform DMDA is not vendored): cell index per axis is
+   floor((x - O)/h), with x == L assigned to the last cell; a coordinate outside [O, L] (or NaN)
+   is not located (-1). */
+static inline int locate_one(const orc_pu *pu, const double *x)
+{
+  int d, c[3] = {0, 0, 0};
+  for (d = 0; d < pu->dim; d++) {
+    double t;
+    if (!(x[d] >= pu->O[d] && x[d] <= pu->L[d])) return -1;
+    t = floor((x[d] - pu->O[d]) / pu->h[d]);
+    c[d] = (int)t;
+    if (c[d] > pu->n[d] - 2) c[d] = pu->n[d] - 2;
+    if (c[d] < 0) c[d] = 0;
+  }
+  if (pu->dim == 2) return c[0] + c[1] * (pu->n[0] - 1);
+  return c[0] + c[1] * (pu->n[0] - 1) + c[2] * (pu->n[0] - 1) * (pu->n[1] - 1);
+}
+
+void orc_locate(const orc_pu *pu, int np, const double *coords, int *cellid)
+{
+  int p;
+  for (p = 0; p < np; p++) cellid[p] = locate_one(pu, &coords[pu->dim * p]);
+}
+
+void orc_cell_csr(const orc_pu *pu, int np, const int *cellid, int *cell_start, int *cell_pts)
+{
+  int c, p;
+  int *fill = (int *)calloc((size_t)pu->ncells + 1, sizeof(int));
+  for (c = 0; c <= pu->ncells; c++) cell_start[c] = 0;
+  for (p = 0; p < np; p++) if (cellid[p] >= 0) cell_start[cellid[p] + 1]++;
+  for (c = 0; c < pu->ncells; c++) cell_start[c + 1] += cell_start[c];
+  for (p = 0; p < np; p++) {
+    int cc = cellid[p];
+    if (cc < 0) continue;
+    cell_pts[cell_start[cc] + fill[cc]++] = p;
+  }
+  free(fill);
+}
+
+/* Inverse map node -> adjacent cells, in ascending cell order (partition.c:54-87). */
+static void node_cells(const orc_pu *pu, int *nc_start, int *nc_list)
+{
+  int e, k, n;
+  int *fill = (int *)calloc((size_t)pu->nnodes, sizeof(int));
+  for (n = 0; n <= pu->nnodes; n++) nc_start[n] = 0;
+  for (e = 0; e < pu->ncells; e++)
+    for (k = 0; k < pu->nen; k++) nc_start[orc_cell_corner(pu, e, k) + 1]++;
+  for (n = 0; n < pu->nnodes; n++) nc_start[n + 1] += nc_start[n];
+  for (e = 0; e < pu->ncells; e++)
+    for (k = 0; k < pu->nen; k++) {
+      int nd = orc_cell_corner(pu, e, k);
+      nc_list[nc_start[nd] + fill[nd]++] = e;
+    }
+  free(fill);
+}
+
+long orc_patch_csr(const orc_pu *pu, const int *cell_start, const int *cell_pts, int *patch_start, int *patch_pts)
+{
+  int n, q;
+  long off = 0;
+  int *nc_start = (int *)malloc(sizeof(int) * ((size_t)pu->nnodes + 1));
+  int *nc_list = (int *)malloc(sizeof(int) * ((size_t)pu->ncells * pu->nen));
+  node_cells(pu, nc_start, nc_list);
+  for (n = 0; n < pu->nnodes; n++) {
+    if (patch_start) patch_start[n] = (int)off;
+    for (q = nc_start[n]; q < nc_start[n + 1]; q++) {
+      int c = nc_list[q];
+      int cnt = cell_start[c + 1] - cell_start[c];
+      if (patch_pts) memcpy(&patch_pts[off], &cell_pts[cell_start[c]], sizeof(int) * (size_t)cnt);
+      off += cnt;
+    }
+  }
+  if (patch_start) patch_start[pu->nnodes] = (int)off;
+  free(nc_start); free(nc_list);
+  return off;
+}
+
+long orc_block_csr(const orc_pu *pu, const int *cell_start, const int *cell_pts, int *blk_start, int *blk_pts)
+{
+  int cx = pu->n[0] - 1, cy = pu->n[1] - 1, cz = (pu->dim == 3) ? pu->n[2] - 1 : 1;
+  int c;
+  long off = 0;
+  for (c = 0; c < pu->ncells; c++) {
+    int l = c / (cx * cy), j = (c - l * cx * cy) / cx, i = c - l * cx * cy - j * cx;
+    int dz, dy, dx, zlo = (pu->dim == 3) ? -1 : 0, zhi = (pu->dim == 3) ? 1 : 0;
+    if (blk_start) blk_start[c] = (int)off;
+    /* neighbour order of CellInfoCreateNeighbourElements_{2D,3D}: ascending linear offset */
+    for (dz = zlo; dz <= zhi; dz++)
+      for (dy = -1; dy <= 1; dy++)
+        for (dx = -1; dx <= 1; dx++) {
+          int ii = i + dx, jj = j + dy, ll = l + dz, nb, cnt;
+          if (ii < 0 || ii >= cx || jj < 0 || jj >= cy || ll < 0 || ll >= cz) continue;
+          nb = ii + jj * cx + ll * cx * cy;
+          cnt = cell_start[nb + 1] - cell_start[nb];
+          if (blk_pts) memcpy(&blk_pts[off], &cell_pts[cell_start[nb]], sizeof(int) * (size_t)cnt);
+          off += cnt;
+        }
+  }
+  if (blk_start) blk_start[pu->ncells] = (int)off;
+  return off;
+}
+
+/* ======================================================================================= */
+/* PU weights: SwarmInterpSetWeights_AVX256 (weights_avx.c:97-243)                          */
+/* ======================================================================================= */
+static inline double wdist_lane(const orc_pu *pu, const double *x, int node)
+{
+  int ix = node % pu->n[0];
+  int iy = (node / pu->n[0]) % pu->n[1];
+  int iz = node / (pu->n[0] * pu->n[1]);
+  double dx = x[0] - node_coord(pu, 0, ix);
+  double dy = x[1] - node_coord(pu, 1, iy);
+  if (pu->dim == 2) return sqrt(fma(dx, dx, dy * dy));
+  {
+    double dz = x[2] - node_coord(pu, 2, iz);
+    return sqrt(fma(dx, dx, fma(dy, dy, dz * dz)));
+  }
+}
+
+static inline double wdist_scalar(const orc_pu *pu, const double *x, int node)
+{
+  int idx[3], d;
+  double dist = 0.0;
+  idx[0] = node % pu->n[0];
+  idx[1] = (node / pu->n[0]) % pu->n[1];
+  idx[2] = node / (pu->n[0] * pu->n[1]);
+  for (d = 0; d < pu->dim; d++) {
+    double c = node_coord(pu, d, idx[d]);
+    dist += (x[d] - c) * (x[d] - c);
+  }
+  return sqrt(dist);
+}
+
+static void weights_one(const orc_pu *pu, const double *x, int cell, double *w)
+{
+  int nen = pu->nen, k, n, l;
+  int corners[8];
+  int aligned = (pu->nnodes / 4) * 4;
+  double sum_w = 0.0;
+  for (k = 0; k < nen; k++) corners[k] = orc_cell_corner(pu, cell, k);
+  for (n = 0; n < aligned; n += 4) {
+    double wa[4];
+    for (l = 0; l < 4; l++) wa[l] = phi_lane(ORC_KERNEL_WENDLAND_C2, wdist_lane(pu, x, n + l), pu->eps_w);
+    sum_w += wa[0] + wa[1] + wa[2] + wa[3];
+    for (k = 0; k < nen; k++) {
+      int nd = corners[k];
+      if (nd == n) w[k] = wa[0];
+      else if (nd == n + 1) w[k] = wa[1];
+      else if (nd == n + 2) w[k] = wa[2];
+      else if (nd == n + 3) w[k] = wa[3];
+    }
+  }
+  for (; n < pu->nnodes; n++) {
+    double weight = orc_phi_scalar(ORC_KERNEL_WENDLAND_C2, wdist_scalar(pu, x, n), pu->eps_w);
+    sum_w += weight;
+    for (k = 0; k < nen; k++) if (corners[k] == n) { w[k] = weight; break; }
+  }
+  for (k = 0; k < nen; k++) {
+    if (sum_w > 0.0) w[k] /= sum_w;
+    else w[k] = 0.0;
+  }
+}
+
+void orc_weights(const orc_pu *pu, int np, const double *coords, const int *cellid, const int *alive,
+                 double *weights)
+{
+  int p;
+  for (p = 0; p < np; p++) {
+    if (alive && !alive[p]) continue;
+    if (cellid[p] < 0) continue;
+    weights_one(pu, &coords[pu->dim * p], cellid[p], &weights[pu->nen * p]);
+  }
+}
+
+/* ======================================================================================= */
+/* patch assembly, factorisation and solve                                                  */
+/* ======================================================================================= */
+static inline double adist_lane(int dim, const double *xi, const double *xj)
+{
+  double dx = xi[0] - xj[0], dy = xi[1] - xj[1];
+  if (dim == 2) return sqrt(fma(dx, dx, dy * dy));
+  {
+    double dz = xi[2] - xj[2];
+    return sqrt(fma(dx, dx, fma(dy, dy, dz * dz)));
+  }
+}
+
+static inline double adist_scalar(int dim, const double *xi, const double *xj)
+{
+  int d;
+  double dist = 0.0;
+  for (d = 0; d < dim; d++) dist += (xi[d] - xj[d]) * (xi[d] - xj[d]);
+  return sqrt(dist);
+}
+
+/* PartitionAssembleRBFMatrix_AVX512, partition_asmb_avx512.c:119-198 (row-major, symmetric). */
+static void assemble(const orc_pu *pu, int kernel, int m, const int *idx, const double *coords, double *A)
+{
+  int i, j, k, dim = pu->dim;
+  double eps = pu->eps_r;
+  for (i = 0; i < m; i++) {
+    const double *xi = &coords[dim * idx[i]];
+    for (j = i; j < (m - 7); j += 8) {
+      for (k = 0; k < 8; k++) {
+        double v = phi_lane(kernel, adist_lane(dim, xi, &coords[dim * idx[j + k]]), eps);
+        A[(size_t)m * i + j + k] = v;
+        if (i != j + k) A[(size_t)m * (j + k) + i] = v;
+      }
+    }
+    for (; j < m; j++) {
+      double v = orc_phi_scalar(kernel, adist_scalar(dim, xi, &coords[dim * idx[j]]), eps);
+      A[(size_t)m * i + j] = v;
+      if (i != j) A[(size_t)m * j + i] = v;
+    }
+  }
+}
+
+/* Lower Cholesky in place (row-major, lower triangle used); left-looking, ascending-k dot
+   products.  LAPACK's blocked dpotrf associates differently; results agree to O(kappa*eps). */
+static int cholesky(int m, double *A)
+{
+  int i, j, k;
+  for (j = 0; j < m; j++) {
+    double d = A[(size_t)m * j + j];
+    for (k = 0; k < j; k++) d -= A[(size_t)m * j + k] * A[(size_t)m * j + k];
+    if (!(d > 0.0)) return j + 1;
+    d = sqrt(d);
+    A[(size_t)m * j + j] = d;
+    for (i = j + 1; i < m; i++) {
+      double s = A[(size_t)m * i + j];
+      for (k = 0; k < j; k++) s -= A[(size_t)m * i + k] * A[(size_t)m * j + k];
+      A[(size_t)m * i + j] = s / d;
+    }
+  }
+  return 0;
+}
+
+static void chol_solve(int m, const double *Lf, double *b)
+{
+  int i, k;
+  for (i = 0; i < m; i++) {
+    double s = b[i];
+    for (k = 0; k < i; k++) s -= Lf[(size_t)m * i + k] * b[k];
+    b[i] = s / Lf[(size_t)m * i + i];
+  }
+  for (i = m - 1; i >= 0; i--) {
+    double s = b[i];
+    for (k = i + 1; k < m; k++) s -= Lf[(size_t)m * k + i] * b[k];
+    b[i] = s / Lf[(size_t)m * i + i];
+  }
+}
+
+/* RHS gather of PartitionMatSetRHS (partition_factor.c:57-90) and MatMatSolve. */
+static void patch_rhs_solve(int m, const int *idx, const double *Lf, int nfields, const double *values, double *coeffs)
+{
+  int f, j;
+  for (f = 0; f < nfields; f++) {
+    double *col = &coeffs[(size_t)f * m];
+    for (j = 0; j < m; j++) col[j] = values[(size_t)idx[j] * nfields + f];
+    chol_solve(m, Lf, col);
+  }
+}
+
+int orc_patch_solve(const orc_pu *pu, int kernel, int m, const int *idx, const double *coords,
+                    int nfields, const double *values, double *coeffs)
+{
+  int info;
+  double *A;
+  if (m == 0) return 0;
+  A = (double *)malloc(sizeof(double) * (size_t)m * m);
+  assemble(pu, kernel, m, idx, coords, A);
+  info = cholesky(m, A);
+  if (!info) patch_rhs_solve(m, idx, A, nfields, values, coeffs);
+  free(A);
+  return info;
+}
+
+/* ======================================================================================= */
+/* evaluation: PointwiseInterpolation_AVX512 (interpolation_avx512.c:121-291)               */
+/* ======================================================================================= */
+static void eval_one(const orc_pu *pu, int kernel, const double *x, int cell, const double *w,
+                     const double *xd, const int *blk_start, const int *blk_pts, const int *patch_start,
+                     const int *patch_pts, const int *patch_setup, double *const *coeffs, int nf,
+                     double *rbf_d, double *val)
+{
+  int dim = pu->dim, nen = pu->nen, k, f, nd, i;
+  int bs = blk_start[cell], bn = blk_start[cell + 1] - bs;
+  const int *bidx = &blk_pts[bs];
+  int aligned;
+  double eps = pu->eps_r;
+  if (bn == 0) return; /* interpolation_avx512.c:184: the value is left untouched */
+  aligned = (bn / 8) * 8;
+  for (nd = 0; nd < aligned; nd += 8)
+    for (i = 0; i < 8; i++) {
+      int dp = bidx[nd + i];
+      double dx = x[0] - xd[dim * dp], dy = x[1] - xd[dim * dp + 1], dist2;
+      if (dim == 2) dist2 = fma(dx, dx, dy * dy);
+      else {
+        double dz = x[2] - xd[dim * dp + 2];
+        dist2 = fma(dx, dx, fma(dy, dy, dz * dz));
+      }
+      rbf_d[dp] = phi_lane(kernel, sqrt(dist2), eps);
+    }
+  for (nd = aligned; nd < bn; nd++) {
+    int dp = bidx[nd], d;
+    double dist = 0.0;
+    for (d = 0; d < dim; d++) { double dx = x[d] - xd[dim * dp + d]; dist += dx * dx; }
+    rbf_d[dp] = orc_phi_scalar(kernel, sqrt(dist), eps);
+  }
+  for (f = 0; f < nf; f++) val[f] = 0.0;
+  for (k = 0; k < nen; k++) {
+    int node = orc_cell_corner(pu, cell, k);
+    int ps = patch_start[node], m = patch_start[node + 1] - ps;
+    const int *didx = &patch_pts[ps];
+    const double *c = coeffs[node];
+    int al;
+    double interp[64];
+    if (!patch_setup[node] || m == 0 || !c) continue; /* ndata == 0 when the patch is not set up */
+    al = (m / 8) * 8;
+    for (f = 0; f < nf; f++) {
+      double l[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+      const double *cf = &c[(size_t)f * m];
+      for (nd = 0; nd < al; nd += 8)
+        for (i = 0; i < 8; i++) l[i] = fma(rbf_d[didx[nd + i]], cf[nd + i], l[i]);
+      /* horizontal sum: 512 -> 256 (lo+hi), 256 -> 128 (lo+hi), hadd */
+      {
+        double s0 = l[0] + l[4], s1 = l[1] + l[5], s2 = l[2] + l[6], s3 = l[3] + l[7];
+        interp[f] = (s0 + s2) + (s1 + s3);
+      }
+    }
+    for (nd = al; nd < m; nd++) {
+      double rbf = rbf_d[didx[nd]];
+      for (f = 0; f < nf; f++) interp[f] += rbf * c[(size_t)f * m + nd];
+    }
+    for (f = 0; f < nf; f++) val[f] += interp[f] * w[k];
+  }
+}
+
+void orc_eval(const orc_pu *pu, int kernel, int np, const double *xp, const int *cellid, const int *alive,
+              const double *weights, const double *xd, const int *blk_start, const int *blk_pts,
+              const int *patch_start, const int *patch_pts, const int *patch_setup, double *const *coeffs,
+              int nf, double *values)
+{
+  int p;
+  long nd = 0;
+  double *rbf_d;
+  /* scratch rbf_d is sized by the largest data index referenced by the blocks */
+  for (p = 0; p < blk_start[pu->ncells]; p++) if (blk_pts[p] + 1 > nd) nd = blk_pts[p] + 1;
+  rbf_d = (double *)calloc((size_t)nd + 1, sizeof(double));
+  for (p = 0; p < np; p++) {
+    if (alive && !alive[p]) continue;
+    if (cellid[p] < 0) continue;
+    eval_one(pu, kernel, &xp[pu->dim * p], cellid[p], &weights[pu->nen * p], xd, blk_start, blk_pts,
+             patch_start, patch_pts, patch_setup, coeffs, nf, rbf_d, &values[(size_t)nf * p]);
+  }
+  free(rbf_d);
+}
+
+/* ======================================================================================= */
+/* reference-API emulation                                                                  */
+/* ======================================================================================= */
+struct orc_ctx {
+  orc_config cfg;
+  orc_pu pu;
+  /* data swarm (swarm_data.c:51-88) */
+  int nd, nd_cap;
+  double *xd, *fd;
+  int64_t *pid_d;
+  int *cell_d, *cell_start, *cell_pts, *blk_start, *blk_pts;
+  int data_binned;
+  /* patches (partition.c) */
+  int *patch_setup, *patch_solved, *patch_start, *patch_pts; /* membership captured at setup */
+  long patch_len;
+  int **patch_idx;       /* per-patch data_idx, owned when set up */
+  int *patch_m;
+  double **coeffs;       /* per-patch column-major coefficients */
+  double **factor;       /* per-patch Cholesky factor kept by A_FACTOR / A_KSP */
+  /* interpolation swarm (swarm_interp.c:72-118) */
+  int np, np_cap;
+  double *xp, *fields, *vel, *weights, *x0, *vadv[7];
+  int64_t *pid_p;
+  int *cell_p, *alive;
+  /* advection */
+  double dt;             /* AdvectionCtx dt; DOPRI writes its adapted step here */
+  double dopri_error;
+  int nsteps;
+  orc_velocity_fn vfn;
+  orc_velocity_batch_fn vfn_batch;
+  void *vuser;
+};
+
+static void *xrealloc(void *p, size_t n) { void *q = realloc(p, n ? n : 1); return q; }
+
+orc_ctx *orc_create(const orc_config *cfg)
+{
+  orc_ctx *c;
+  int n;
+  if (cfg->dim != 2 && cfg->dim != 3) return NULL; /* cell_info.c:312-324 */
+  for (n = 0; n < cfg->dim; n++) if (cfg->n[n] < 2) return NULL;
+  c = (orc_ctx *)calloc(1, sizeof(*c));
+  c->cfg = *cfg;
+  orc_pu_setup(&c->pu, cfg);
+  c->patch_setup = (int *)calloc((size_t)c->pu.nnodes, sizeof(int));
+  c->patch_solved = (int *)calloc((size_t)c->pu.nnodes, sizeof(int));
+  c->patch_idx = (int **)calloc((size_t)c->pu.nnodes, sizeof(int *));
+  c->patch_m = (int *)calloc((size_t)c->pu.nnodes, sizeof(int));
+  c->coeffs = (double **)calloc((size_t)c->pu.nnodes, sizeof(double *));
+  c->factor = (double **)calloc((size_t)c->pu.nnodes, sizeof(double *));
+  c->patch_start = (int *)calloc((size_t)c->pu.nnodes + 1, sizeof(int));
+  c->cell_start = (int *)calloc((size_t)c->pu.ncells + 1, sizeof(int));
+  c->blk_start = (int *)calloc((size_t)c->pu.ncells + 1, sizeof(int));
+  c->dt = cfg->dt;
+  c->dopri_error = ORC_MAX_REAL;
+  return c;
+}
+
+static void patch_reset_one(orc_ctx *c, int n)
+{
+  /* PartitionReset_SinglePartition, partition.c:235-250 */
+  c->patch_solved[n] = 0;
+  c->patch_setup[n] = 0;
+  free(c->patch_idx[n]); c->patch_idx[n] = NULL; c->patch_m[n] = 0;
+  free(c->coeffs[n]); c->coeffs[n] = NULL;
+  free(c->factor[n]); c->factor[n] = NULL;
+}
+
+void orc_destroy(orc_ctx *c)
+{
+  int n, s;
+  if (!c) return;
+  for (n = 0; n < c->pu.nnodes; n++) patch_reset_one(c, n);
+  free(c->patch_setup); free(c->patch_solved); free(c->patch_idx); free(c->patch_m);
+  free(c->coeffs); free(c->factor); free(c->patch_start); free(c->patch_pts);
+  free(c->xd); free(c->fd); free(c->pid_d); free(c->cell_d); free(c->cell_start); free(c->cell_pts);
+  free(c->blk_start); free(c->blk_pts);
+  free(c->xp); free(c->fields); free(c->vel); free(c->weights); free(c->x0);
+  for (s = 0; s < 7; s++) free(c->vadv[s]);
+  free(c->pid_p); free(c->cell_p); free(c->alive);
+  free(c);
+}
+
+/* SwarmFieldAssignUniqueIndex (swarm_utils.c:37-73) on one rank: pid = max(existing) + 1 + p,
+   where "existing" are the values the resized swarm still holds (DMSwarmSetLocalSizes keeps the
+   first min(old,new) entries and zeroes the rest). */
+static void assign_pid(int64_t *pid, int old_n, int new_n)
+{
+  int p;
+  int64_t mx = 0;
+  for (p = 0; p < new_n; p++) {
+    int64_t v = (p < old_n) ? pid[p] : 0;
+    if (v > mx) mx = v;
+  }
+  mx += 1;
+  for (p = 0; p < new_n; p++) pid[p] = mx + p;
+}
+
+static int check_inside_box(const orc_pu *pu, int n, const double *coords)
+{
+  /* DMSwarmAssignRankFromDMDA (swarm_utils.c:854-871): a point outside the bounding box of the
+     (single-rank) DMDA is an error. */
+  int p, d;
+  for (p = 0; p < n; p++)
+    for (d = 0; d < pu->dim; d++) {
+      double x = coords[pu->dim * p + d];
+      if (x < pu->O[d] || x > pu->L[d]) return ORC_ERR_ARG_WRONG;
+    }
+  return 0;
+}
+
+int orc_fill_swarm(orc_ctx *c, int is_data, int n, const double *coords, const double *values,
+                   const int64_t *pidx)
+{
+  int dim = c->pu.dim, F = c->cfg.nfields, nen = c->pu.nen, p, s;
+  if (n < 0) return ORC_ERR_ARG_OUTOFRANGE;
+  if (n > 0 && !coords) return ORC_ERR_ARG_NULL;
+  if (check_inside_box(&c->pu, n, coords)) return ORC_ERR_ARG_WRONG;
+  if (is_data) {
+    int old = c->nd;
+    c->xd = (double *)xrealloc(c->xd, sizeof(double) * (size_t)n * dim);
+    c->fd = (double *)xrealloc(c->fd, sizeof(double) * (size_t)n * (F ? F : 1));
+    c->pid_d = (int64_t *)xrealloc(c->pid_d, sizeof(int64_t) * (size_t)(n ? n : 1));
+    for (p = old; p < n; p++) c->pid_d[p] = 0;
+    if (n > old) memset(&c->fd[(size_t)old * F], 0, sizeof(double) * (size_t)(n - old) * F);
+    c->cell_d = (int *)xrealloc(c->cell_d, sizeof(int) * (size_t)(n ? n : 1));
+    c->cell_pts = (int *)xrealloc(c->cell_pts, sizeof(int) * (size_t)(n ? n : 1));
+    if (n) memcpy(c->xd, coords, sizeof(double) * (size_t)n * dim);
+    if (values && n) memcpy(c->fd, values, sizeof(double) * (size_t)n * F);
+    if (pidx) { if (n) memcpy(c->pid_d, pidx, sizeof(int64_t) * (size_t)n); }
+    else assign_pid(c->pid_d, old, n);
+    c->nd = n;
+    /* DMSwarmPICSetCellId + CellInfoSetUp (interface_utils.c:140-165) */
+    orc_locate(&c->pu, n, c->xd, c->cell_d);
+    orc_cell_csr(&c->pu, n, c->cell_d, c->cell_start, c->cell_pts);
+    {
+      long bl = orc_block_csr(&c->pu, c->cell_start, c->cell_pts, NULL, NULL);
+      c->blk_pts = (int *)xrealloc(c->blk_pts, sizeof(int) * (size_t)(bl ? bl : 1));
+      orc_block_csr(&c->pu, c->cell_start, c->cell_pts, c->blk_start, c->blk_pts);
+    }
+    c->data_binned = 1;
+    return 0;
+  }
+  {
+    int old = c->np;
+    c->xp = (double *)xrealloc(c->xp, sizeof(double) * (size_t)n * dim);
+    c->fields = (double *)xrealloc(c->fields, sizeof(double) * (size_t)n * (F ? F : 1));
+    c->vel = (double *)xrealloc(c->vel, sizeof(double) * (size_t)n * dim);
+    c->weights = (double *)xrealloc(c->weights, sizeof(double) * (size_t)n * nen);
+    c->x0 = (double *)xrealloc(c->x0, sizeof(double) * (size_t)n * dim);
+    for (s = 0; s < 7; s++) c->vadv[s] = (double *)xrealloc(c->vadv[s], sizeof(double) * (size_t)n * dim);
+    c->pid_p = (int64_t *)xrealloc(c->pid_p, sizeof(int64_t) * (size_t)(n ? n : 1));
+    c->cell_p = (int *)xrealloc(c->cell_p, sizeof(int) * (size_t)(n ? n : 1));
+    c->alive = (int *)xrealloc(c->alive, sizeof(int) * (size_t)(n ? n : 1));
+    for (p = old; p < n; p++) c->pid_p[p] = 0;
+    if (n > old) {
+      memset(&c->fields[(size_t)old * F], 0, sizeof(double) * (size_t)(n - old) * F);
+      memset(&c->vel[(size_t)old * dim], 0, sizeof(double) * (size_t)(n - old) * dim);
+      memset(&c->weights[(size_t)old * nen], 0, sizeof(double) * (size_t)(n - old) * nen);
+    }
+    if (n) memcpy(c->xp, coords, sizeof(double) * (size_t)n * dim);
+    if (values && n) memcpy(c->fields, values, sizeof(double) * (size_t)n * F);
+    if (pidx) { if (n) memcpy(c->pid_p, pidx, sizeof(int64_t) * (size_t)n); }
+    else assign_pid(c->pid_p, old, n);
+    c->np = n;
+    for (p = 0; p < n; p++) c->alive[p] = 1;
+    /* FillInterpSwarm (interface_utils.c:118-138): cell ids + weights */
+    orc_locate(&c->pu, n, c->xp, c->cell_p);
+    orc_weights(&c->pu, n, c->xp, c->cell_p, c->alive, c->weights);
+    return 0;
+  }
+}
+
+/* Lazy patch set-up and solve (LagRBF_PartitionsSetUp, partition.c:417-478). */
+static int partitions_setup(orc_ctx *c)
+{
+  int p, k, F = c->cfg.nfields;
+  for (p = 0; p < c->np; p++) {
+    if (!c->alive[p] || c->cell_p[p] < 0) continue;
+    for (k = 0; k < c->pu.nen; k++) {
+      int node = orc_cell_corner(&c->pu, c->cell_p[p], k);
+      if (!c->patch_setup[node]) {
+        /* PartitionSetUp_SinglePartition: membership from the current data-swarm sort */
+        long len = orc_patch_csr(&c->pu, c->cell_start, c->cell_pts, NULL, NULL);
+        int m, info;
+        if (len != c->patch_len || !c->patch_pts) {
+          c->patch_pts = (int *)xrealloc(c->patch_pts, sizeof(int) * (size_t)(len ? len : 1));
+          c->patch_len = len;
+        }
+        orc_patch_csr(&c->pu, c->cell_start, c->cell_pts, c->patch_start, c->patch_pts);
+        m = c->patch_start[node + 1] - c->patch_start[node];
+        c->patch_idx[node] = (int *)malloc(sizeof(int) * (size_t)(m ? m : 1));
+        if (m) memcpy(c->patch_idx[node], &c->patch_pts[c->patch_start[node]], sizeof(int) * (size_t)m);
+        c->patch_m[node] = m;
+        c->coeffs[node] = (double *)calloc((size_t)(m ? m : 1) * (F ? F : 1), sizeof(double));
+        if (m) {
+          double *A = (double *)malloc(sizeof(double) * (size_t)m * m);
+          assemble(&c->pu, c->cfg.kernel, m, c->patch_idx[node], c->xd, A);
+          info = cholesky(m, A);
+          if (info) { free(A); return ORC_ERR_MAT_CH_ZRPVT; }
+          c->factor[node] = A;
+        }
+        c->patch_setup[node] = 1;
+      }
+      if (!c->patch_solved[node]) {
+        /* PartitionSolveInterpolationCoefficients_SinglePartition, partition_solve.c:97-113 */
+        int m = c->patch_m[node];
+        if (m > 0) {
+          patch_rhs_solve(m, c->patch_idx[node], c->factor[node], F, c->fd, c->coeffs[node]);
+          if (c->cfg.solve_method == ORC_A_KSP_ASMB || c->cfg.solve_method == ORC_A_FACTOR) {
+            /* the assembled/factored matrix is released after the solve; A_FACTOR reloads its
+               factor from disk on the next solve, which keeping it here reproduces */
+            if (c->cfg.solve_method == ORC_A_KSP_ASMB) { free(c->factor[node]); c->factor[node] = NULL; }
+          }
+          c->patch_solved[node] = 1;
+        }
+      }
+    }
+  }
+  return 0;
+}
+
+/* Evaluation over all live particles of the interpolation swarm. */
+static void rbf_interpolation(orc_ctx *c, int nf, double *values)
+{
+  int node;
+  long len = 0;
+  int *ps, *pp, *setup;
+  double **cf;
+  /* per-patch arrays captured at set-up time */
+  ps = (int *)malloc(sizeof(int) * ((size_t)c->pu.nnodes + 1));
+  setup = (int *)malloc(sizeof(int) * (size_t)c->pu.nnodes);
+  cf = (double **)malloc(sizeof(double *) * (size_t)c->pu.nnodes);
+  for (node = 0; node < c->pu.nnodes; node++) { ps[node] = (int)len; len += c->patch_setup[node] ? c->patch_m[node] : 0; }
+  ps[c->pu.nnodes] = (int)len;
+  pp = (int *)malloc(sizeof(int) * (size_t)(len ? len : 1));
+  for (node = 0; node < c->pu.nnodes; node++) {
+    setup[node] = c->patch_setup[node];
+    cf[node] = c->patch_setup[node] ? c->coeffs[node] : NULL;
+    if (c->patch_setup[node] && c->patch_m[node])
+      memcpy(&pp[ps[node]], c->patch_idx[node], sizeof(int) * (size_t)c->patch_m[node]);
+  }
+  orc_eval(&c->pu, c->cfg.kernel, c->np, c->xp, c->cell_p, c->alive, c->weights, c->xd, c->blk_start,
+           c->blk_pts, ps, pp, setup, cf, nf, values);
+  free(ps); free(pp); free(setup); free(cf);
+}
+
+int orc_interpolation(orc_ctx *c)
+{
+  int err;
+  if (!c->data_binned) return ORC_ERR_ARG_NULL;
+  err = partitions_setup(c);
+  if (err) return err;
+  rbf_interpolation(c, c->cfg.nfields, c->fields);
+  return 0;
+}
+
+int orc_output(orc_ctx *c, int is_data, int nglobal, double *coords, double *fields, int64_t *pidx,
+               const char *fieldname)
+{
+  /* Interface_Output_Allreduce / AssembleArray_Allreduce (interface_utils.c:188-339) */
+  int dim = c->pu.dim, n = is_data ? c->nd : c->np, p, f, nf = 0;
+  const int64_t *pid = is_data ? c->pid_d : c->pid_p;
+  const double *src = NULL;
+  if (fields) {
+    if (!fieldname || strcmp(fieldname, "fields") == 0) { src = is_data ? c->fd : c->fields; nf = c->cfg.nfields; }
+    else if (!is_data && strcmp(fieldname, "velocity") == 0) { src = c->vel; nf = dim; }
+    else if (!is_data && strcmp(fieldname, "weights") == 0) { src = c->weights; nf = c->pu.nen; }
+    else return ORC_ERR_ARG_WRONG;
+  }
+  if (coords) memset(coords, 0, sizeof(double) * (size_t)nglobal * dim);
+  if (fields) memset(fields, 0, sizeof(double) * (size_t)nglobal * nf);
+  if (pidx) memset(pidx, 0, sizeof(int64_t) * (size_t)nglobal);
+  for (p = 0; p < n; p++) {
+    int64_t g;
+    if (!is_data && !c->alive[p]) continue; /* removed by migration */
+    g = pid[p] - 1;
+    if (g < 0 || g >= nglobal) return ORC_ERR_ARG_OUTOFRANGE;
+    if (coords) for (f = 0; f < dim; f++) coords[g * dim + f] = (is_data ? c->xd : c->xp)[(size_t)p * dim + f];
+    if (fields) for (f = 0; f < nf; f++) fields[g * nf + f] = src[(size_t)p * nf + f];
+    if (pidx) pidx[g] = pid[p];
+  }
+  return 0;
+}
+
+int orc_reset_coefficients(orc_ctx *c)
+{
+  int n;
+  for (n = 0; n < c->pu.nnodes; n++) {
+    if (c->cfg.solve_method == ORC_A_KSP_ASMB) patch_reset_one(c, n);
+    else c->patch_solved[n] = 0;
+  }
+  return 0;
+}
+
+/* --------------------------------- advection ---------------------------------------- */
+/* AdvectionProjectOntoSphereBoundary_Pointwise (advection.c:472-491) */
+static void project_sphere(double *x, int dim, double rmin, double rmax)
+{
+  int d;
+  double pos = 0.0, normal[3];
+  for (d = 0; d < dim; d++) pos += x[d] * x[d];
+  if (pos < rmax * rmax && pos > rmin * rmin) return;
+  pos = sqrt(pos);
+  for (d = 0; d < dim; d++) normal[d] = x[d] / pos;
+  if (pos > rmax) for (d = 0; d < dim; d++) x[d] = rmax * normal[d];
+  else for (d = 0; d < dim; d++) x[d] = rmin * normal[d];
+}
+
+/* DMSwarmMigrate on one rank: relocate, drop particles that left the domain; then
+   SwarmInterpSetWeights. */
+static void migrate_and_weights(orc_ctx *c)
+{
+  int p;
+  orc_locate(&c->pu, c->np, c->xp, c->cell_p);
+  for (p = 0; p < c->np; p++) if (c->alive[p] && c->cell_p[p] < 0) c->alive[p] = 0;
+  orc_weights(&c->pu, c->np, c->xp, c->cell_p, c->alive, c->weights);
+}
+
+static int evaluate_velocity(orc_ctx *c)
+{
+  /* AdvectionEvaluateVelocity (advection.c:391-414) */
+  int dim = c->pu.dim, p;
+  if (c->vfn_batch || c->vfn) {
+    /* analytical: the callback sees the live particles packed contiguously */
+    int nl = 0, q = 0, err = 0;
+    double *xc, *vc;
+    for (p = 0; p < c->np; p++) nl += c->alive[p];
+    xc = (double *)malloc(sizeof(double) * (size_t)(nl ? nl : 1) * dim);
+    vc = (double *)malloc(sizeof(double) * (size_t)(nl ? nl : 1) * dim);
+    for (p = 0; p < c->np; p++) if (c->alive[p]) { memcpy(&xc[(size_t)q * dim], &c->xp[(size_t)p * dim], sizeof(double) * dim); q++; }
+    memset(vc, 0, sizeof(double) * (size_t)(nl ? nl : 1) * dim);
+    if (c->vfn_batch) err = c->vfn_batch(nl, dim, xc, vc, c->vuser);
+    else for (q = 0; q < nl && !err; q++) err = c->vfn(&xc[(size_t)q * dim], &vc[(size_t)q * dim], c->vuser);
+    q = 0;
+    for (p = 0; p < c->np; p++) if (c->alive[p]) { memcpy(&c->vel[(size_t)p * dim], &vc[(size_t)q * dim], sizeof(double) * dim); q++; }
+    free(xc); free(vc);
+    return err;
+  }
+  rbf_interpolation(c, dim, c->vel);
+  return 0;
+}
+
+static void copy_fields_to_velocity(orc_ctx *c)
+{
+  /* AdvectionCopyVelocityField (advection.c:298-316) */
+  int p, d, dim = c->pu.dim, F = c->cfg.nfields;
+  for (p = 0; p < c->np; p++)
+    for (d = 0; d < dim; d++) c->vel[(size_t)p * dim + d] = (d < F) ? c->fields[(size_t)p * F + d] : 0.0;
+}
+
+static int initialize_timestep_velocity(orc_ctx *c)
+{
+  /* AdvectionInitializeTimestepVelocity (advection.c:353-373) */
+  if (c->vfn_batch || c->vfn) return evaluate_velocity(c);
+  copy_fields_to_velocity(c);
+  return 0;
+}
+
+static void euler(orc_ctx *c, double *x, const double *x0, const double *v, double dt)
+{
+  /* AdvectionExplicit_Scalar (advection.c:36-57) */
+  int p, d, dim = c->pu.dim;
+  for (p = 0; p < c->np; p++) {
+    if (!c->alive[p]) continue;
+    for (d = 0; d < dim; d++) x[(size_t)p * dim + d] = x0[(size_t)p * dim + d] + dt * v[(size_t)p * dim + d];
+  }
+}
+
+static int rk1(orc_ctx *c)
+{
+  /* runge_kutta_1.c:37-75 */
+  int dim = c->pu.dim;
+  memcpy(c->x0, c->xp, sizeof(double) * (size_t)c->np * dim);
+  euler(c, c->xp, c->x0, c->vel, c->dt);
+  migrate_and_weights(c);
+  return 0;
+}
+
+static int rk2(orc_ctx *c)
+{
+  /* runge_kutta_2.c:38-91 */
+  int dim = c->pu.dim, err;
+  memcpy(c->x0, c->xp, sizeof(double) * (size_t)c->np * dim);
+  euler(c, c->xp, c->x0, c->vel, 0.5 * c->dt);
+  migrate_and_weights(c);
+  if ((err = evaluate_velocity(c))) return err;
+  euler(c, c->xp, c->x0, c->vel, c->dt);
+  migrate_and_weights(c);
+  return 0;
+}
+
+static void set_initial_values(orc_ctx *c)
+{
+  /* AdvectionSetInitialValues (advection.c:248-278) */
+  int dim = c->pu.dim;
+  memcpy(c->x0, c->xp, sizeof(double) * (size_t)c->np * dim);
+  memcpy(c->vadv[0], c->vel, sizeof(double) * (size_t)c->np * dim);
+}
+
+static int rk4(orc_ctx *c)
+{
+  /* runge_kutta_4.c:45-156 */
+  static const double coef[3] = {0.5, 0.5, 1.0};
+  static const double wts[4] = {1.0, 2.0, 2.0, 1.0};
+  int dim = c->pu.dim, s, p, d, err;
+  double dt = c->dt;
+  set_initial_values(c);
+  for (s = 0; s < 3; s++) {
+    memcpy(c->vel, c->vadv[s], sizeof(double) * (size_t)c->np * dim);
+    euler(c, c->xp, c->x0, c->vel, coef[s] * dt);
+    for (p = 0; p < c->np; p++) if (c->alive[p]) project_sphere(&c->xp[(size_t)p * dim], dim, c->cfg.rmin, c->cfg.rmax);
+    migrate_and_weights(c);
+    if ((err = evaluate_velocity(c))) return err;
+    memcpy(c->vadv[s + 1], c->vel, sizeof(double) * (size_t)c->np * dim);
+  }
+  for (p = 0; p < c->np; p++) {
+    double sum[3] = {0.0, 0.0, 0.0};
+    if (!c->alive[p]) continue;
+    for (d = 0; d < dim; d++) {
+      for (s = 0; s < 4; s++) sum[d] += wts[s] * c->vadv[s][(size_t)p * dim + d];
+      c->xp[(size_t)p * dim + d] = c->x0[(size_t)p * dim + d] + dt / 6.0 * sum[d];
+      /* runge_kutta_4.c:140: projection inside the per-component loop */
+      project_sphere(&c->xp[(size_t)p * dim], dim, c->cfg.rmin, c->cfg.rmax);
+    }
+  }
+  migrate_and_weights(c);
+  return 0;
+}
+
+static const double DP_A[6][6] = {
+  {1.0 / 5.0, 0, 0, 0, 0, 0},
+  {3.0 / 40.0, 9.0 / 40.0, 0, 0, 0, 0},
+  {44.0 / 45.0, -56.0 / 15.0, 32.0 / 9.0, 0, 0, 0},
+  {19372.0 / 6561.0, -25360.0 / 2187.0, 64448.0 / 6561.0, -212.0 / 729.0, 0, 0},
+  {9017.0 / 3168.0, -355.0 / 33.0, 46732.0 / 5247.0, 49.0 / 176.0, -5103.0 / 18656.0, 0},
+  {35.0 / 384.0, 0, 500.0 / 1113.0, 125.0 / 192.0, -2187.0 / 6784.0, 11.0 / 84.0}};
+static const double DP_E[7] = {5179.0 / 57600.0, 0, 7571.0 / 16695.0, 393.0 / 640.0, -92097.0 / 339200.0,
+                               187.0 / 2100.0, 1.0 / 40.0};
+
+static int dopri(orc_ctx *c)
+{
+  /* dormand_prince.c:216-310 (Butcher rows :224-231), error :37-102, adaptive dt :179-214 */
+  int dim = c->pu.dim, s, j, p, d, err;
+  double dt = c->dt, max_err, fac, fac_min, fac_max, dt_new;
+  set_initial_values(c);
+  for (s = 0; s < 6; s++) {
+    int stage = s + 1;
+    for (p = 0; p < c->np; p++) {
+      if (!c->alive[p]) { for (d = 0; d < dim; d++) c->vel[(size_t)p * dim + d] = 0.0; continue; }
+      for (d = 0; d < dim; d++) c->vel[(size_t)p * dim + d] = 0.0;
+      for (j = 0; j < stage; j++)
+        for (d = 0; d < dim; d++) c->vel[(size_t)p * dim + d] += DP_A[s][j] * c->vadv[j][(size_t)p * dim + d];
+      for (d = 0; d < dim; d++) c->xp[(size_t)p * dim + d] = c->x0[(size_t)p * dim + d] + dt * c->vel[(size_t)p * dim + d];
+      project_sphere(&c->xp[(size_t)p * dim], dim, c->cfg.rmin, c->cfg.rmax);
+    }
+    migrate_and_weights(c);
+    if ((err = evaluate_velocity(c))) return err;
+    memcpy(c->vadv[stage], c->vel, sizeof(double) * (size_t)c->np * dim);
+  }
+  max_err = -ORC_MAX_REAL; /* PETSC_MIN_REAL */
+  for (p = 0; p < c->np; p++) {
+    double vlow[3] = {0.0, 0.0, 0.0}, E = 0.0;
+    if (!c->alive[p]) continue;
+    for (s = 0; s < 7; s++)
+      for (d = 0; d < dim; d++) vlow[d] += DP_E[s] * c->vadv[s][(size_t)p * dim + d];
+    for (d = 0; d < dim; d++) {
+      double x0 = c->x0[(size_t)p * dim + d], x = c->xp[(size_t)p * dim + d];
+      double mv = ORC_MAX(fabs(x0), fabs(x));
+      double tol = c->cfg.dopri_atol + c->cfg.dopri_rtol * mv;
+      double xl = x0 + dt * vlow[d];
+      double e = x - xl;
+      E += (e * e) / (tol * tol);
+    }
+    E = sqrt(1.0 / dim * E);
+    max_err = ORC_MAX(max_err, E);
+  }
+  c->dopri_error = max_err;
+  migrate_and_weights(c);
+  fac = c->cfg.dopri_dt_fac;
+  fac_min = c->cfg.dopri_dt_fac_min;
+  fac_max = (max_err <= 1.0) ? c->cfg.dopri_dt_fac_max : 1.0;
+  dt_new = dt * ORC_MIN(fac_max, ORC_MAX(fac_min, fac * pow(1.0 / max_err, 1.0 / 5.0)));
+  c->dt = dt_new;
+  return 0;
+}
+
+static int advect_swarm(orc_ctx *c)
+{
+  switch (c->cfg.scheme) {
+  case ORC_RK1: return rk1(c);
+  case ORC_RK2: return rk2(c);
+  case ORC_RK4: return rk4(c);
+  case ORC_DOPRI: return dopri(c);
+  default: return ORC_ERR_ARG_OUTOFRANGE;
+  }
+}
+
+static double cfl_dt(orc_ctx *c)
+{
+  /* AdvectionComputeTimestep_CFL (advection.c:430-470) */
+  int p, d, dim = c->pu.dim;
+  double radius = 1.0 / c->pu.eps_w, dt = ORC_MAX_REAL;
+  for (p = 0; p < c->np; p++) {
+    double nv = 0.0, dl;
+    if (!c->alive[p]) continue;
+    for (d = 0; d < dim; d++) nv += c->vel[(size_t)p * dim + d] * c->vel[(size_t)p * dim + d];
+    nv = sqrt(nv);
+    dl = c->cfg.cfl_fac * radius / (nv + 1e-16);
+    dt = ORC_MIN(dt, dl);
+  }
+  return dt;
+}
+
+static int advection_loop(orc_ctx *c, double t, double t_next, int interpolated, int keep)
+{
+  /* InternalForwardAdvectionLoop (time_loop.c:39-100) / ForwardAnalyticalAdvection (:176-221) */
+  int err;
+  if ((err = initialize_timestep_velocity(c))) return err;
+  while (t < t_next) {
+    double dt;
+    if (c->cfg.scheme == ORC_DOPRI) {
+      double dt_cfl = cfl_dt(c);
+      dt = ORC_MIN(c->dt, dt_cfl);
+    } else dt = cfl_dt(c);
+    if (t + dt > t_next) dt = t_next - t;
+    c->dt = dt;
+    if ((err = advect_swarm(c))) return err;
+    if (interpolated) {
+      if ((err = partitions_setup(c))) return err;
+      rbf_interpolation(c, c->cfg.nfields, c->fields);
+    }
+    if ((err = initialize_timestep_velocity(c))) return err;
+    t += dt;
+    c->nsteps++;
+  }
+  if (interpolated && !keep) {
+    orc_reset_coefficients(c);
+    /* CellInfoReset + clearing the data swarm (time_loop.c:94-98) */
+    c->nd = 0;
+    c->data_binned = 0;
+  }
+  return 0;
+}
+
+int orc_advect_interpolate(orc_ctx *c, double t, double t_next)
+{
+  if (!c->data_binned) return ORC_ERR_ARG_NULL;
+  if (c->vfn || c->vfn_batch) return ORC_ERR_ARG_WRONGSTATE;
+  return advection_loop(c, t, t_next, 1, 0);
+}
+
+int orc_advect_analytical(orc_ctx *c, double t, double t_next)
+{
+  if (!c->vfn && !c->vfn_batch) return ORC_ERR_ARG_NULL;
+  return advection_loop(c, t, t_next, 0, 0);
+}
+
+int orc_set_velocity_fn(orc_ctx *c, orc_velocity_fn fn, void *user) { c->vfn = fn; c->vuser = user; return 0; }
+int orc_set_velocity_batch_fn(orc_ctx *c, orc_velocity_batch_fn fn, void *user) { c->vfn_batch = fn; c->vuser = user; return 0; }
+
+int orc_get_counts(orc_ctx *c, int *nd, int *np_alive, int *npatch_setup, int *nsteps)
+{
+  int p, n = 0, s = 0;
+  for (p = 0; p < c->np; p++) n += c->alive[p];
+  for (p = 0; p < c->pu.nnodes; p++) s += c->patch_setup[p];
+  if (nd) *nd = c->nd;
+  if (np_alive) *np_alive = n;
+  if (npatch_setup) *npatch_setup = s;
+  if (nsteps) *nsteps = c->nsteps;
+  return 0;
+}
+
+double orc_get_dt(orc_ctx *c) { return c->dt; }
+
+int orc_get_cellids(orc_ctx *c, int is_data, int *cellid)
+{
+  int n = is_data ? c->nd : c->np;
+  memcpy(cellid, is_data ? c->cell_d : c->cell_p, sizeof(int) * (size_t)n);
+  return n;
+}
+
+long orc_get_patch_csr(orc_ctx *c, int *patch_start, int *patch_pts)
+{
+  return orc_patch_csr(&c->pu, c->cell_start, c->cell_pts, patch_start, patch_pts);
+}
+
+long orc_get_block_csr(orc_ctx *c, int *blk_start, int *blk_pts)
+{
+  return orc_block_csr(&c->pu, c->cell_start, c->cell_pts, blk_start, blk_pts);
+}
+
+int orc_get_weights(orc_ctx *c, double *weights)
+{
+  memcpy(weights, c->weights, sizeof(double) * (size_t)c->np * c->pu.nen);
+  return c->np;
+}
+
+/* ======================================================================================= */
+/* CPU baseline timing                                                                      */
+/* ======================================================================================= */
+static double now_s(void)
+{
+  struct timespec ts;
+  clock_gettime(CLOCK_MONOTONIC, &ts);
+  return ts.tv_sec + 1e-9 * ts.tv_nsec;
+}
+
+int orc_time_baseline(const orc_config *cfg, int nd, const double *xd, const double *fd, int np,
+                      const double *xp, int nsteps, double dt, int nthreads, double *setup_s, double *step_s)
+{
+  int err = 0;
+  double t0, t1, t2;
+  int r;
+  orc_ctx **ctxs;
+  if (nthreads < 1) nthreads = 1;
+  ctxs = (orc_ctx **)calloc((size_t)nthreads, sizeof(orc_ctx *));
+  t0 = now_s();
+  /* one emulated rank per thread: same dataset, disjoint particle subsets */
+#pragma omp parallel for num_threads(nthreads) schedule(static, 1) reduction(| : err)
+  for (r = 0; r < nthreads; r++) {
+    int lo = (int)((long)np * r / nthreads), hi = (int)((long)np * (r + 1) / nthreads), e;
+    orc_ctx *c = orc_create(cfg);
+    ctxs[r] = c;
+    if (!c) { err |= 1; continue; }
+    e = orc_fill_swarm(c, 1, nd, xd, fd, NULL);
+    if (!e) e = orc_fill_swarm(c, 0, hi - lo, &xp[(size_t)lo * cfg->dim], NULL, NULL);
+    if (!e) e = orc_interpolation(c);
+    err |= e;
+  }
+  t1 = now_s();
+#pragma omp parallel for num_threads(nthreads) schedule(static, 1) reduction(| : err)
+  for (r = 0; r < nthreads; r++) {
+    orc_ctx *c = ctxs[r];
+    int s, e = 0;
+    double t = 0.0;
+    if (!c) continue;
+    /* steady state: the dataset, its binning and the patch factors stay resident (A_KSP) */
+    for (s = 0; s < nsteps && !e; s++) {
+      e = advection_loop(c, t, t + dt, 1, 1);
+      t += dt;
+    }
+    err |= e;
+  }
+  t2 = now_s();
+  for (r = 0; r < nthreads; r++) orc_destroy(ctxs[r]);
+  free(ctxs);
+  if (setup_s) *setup_s = t1 - t0;
+  if (step_s) *step_s = t2 - t1;
+  return err;
+}

@@ -1,0 +1,262 @@
+"""GPU parity tests: the CUDA path (through the C-ABI) against the CPU oracle on the same seeded
+inputs.  Tolerances: bit-exact for cell ids, patch membership and evaluation blocks; max-normalised
+relative error <= 1e-10 for the FP64 path against the oracle; <= 1e-6 for the FP32-evaluation path
+against the FP64 path.  Max-normalised: max_p |a_p - b_p| / max_p |b_p| per component.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+from oracle_lib import Oracle
+import lagrbf_gb300 as L
+from lagrbf_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+TOL64 = 1e-10
+TOL32 = 1e-6
+
+
+def relerr(a, b):
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    den = np.abs(b).max(axis=0)
+    den[den == 0] = 1.0
+    return float((np.abs(a - b).max(axis=0) / den).max())
+
+
+def small_3d(nlat=20, npu=5, np_=3000, seed=11, field="abc"):
+    rng = np.random.default_rng(seed)
+    xd = W.jittered_lattice(nlat, 3, rng)
+    fd = W.abc_flow(xd) if field == "abc" else W.fourier_field(xd, rng)
+    xp = W.uniform_points(np_, 3, np.random.default_rng(seed + 1))
+    opts = dict(dim=3, npartitions=[npu] * 3, overlap=W.pu_overlap(npu), shape_factor=1.0, kernel=2, nfields=3)
+    return xd, fd, xp, opts
+
+
+def small_2d(nlat=32, npu=6, np_=2000, seed=5, kernel=2):
+    rng = np.random.default_rng(seed)
+    xd = W.jittered_lattice(nlat, 2, rng)
+    fd = W.cellular_flow(xd)
+    xp = W.uniform_points(np_, 2, np.random.default_rng(seed + 1))
+    opts = dict(dim=2, npartitions=[npu] * 2, overlap=W.pu_overlap(npu), shape_factor=1.0, kernel=kernel, nfields=2)
+    return xd, fd, xp, opts
+
+
+def gpu_ctx(opts, **extra):
+    o = dict(opts)
+    o.update(extra)
+    return L.LagRBFCtx(**o)
+
+
+def gpu_output(c, n, nf, fieldname="fields"):
+    x = np.zeros((n, c.dim))
+    f = np.zeros((n, nf))
+    p = np.zeros(n, dtype=np.int64)
+    c.output(coords=x, fvals=f, pidx=p, fieldname=fieldname)
+    return x, f, p
+
+
+@pytest.mark.parametrize("case", ["3d", "2d"])
+def test_binning_bit_exact(case):
+    xd, fd, xp, opts = small_3d() if case == "3d" else small_2d()
+    # points exactly on faces and on the upper boundary
+    extra = np.array([[1.0] * opts["dim"], [0.0] * opts["dim"], [0.5] * opts["dim"]])
+    xp = np.concatenate([xp, extra])
+    c = gpu_ctx(opts)
+    o = Oracle(**opts)
+    c.fill_data(xd, fd)
+    c.fill_points(xp)
+    assert o.fill(True, xd, fd) == 0 and o.fill(False, xp) == 0
+    assert np.array_equal(c.cellids(True, len(xd)), o.cellids(True, len(xd)))
+    assert np.array_equal(c.cellids(False, len(xp)), o.cellids(False, len(xp)))
+    ints, _ = c.geometry()
+    s1, p1 = c.patch_csr()
+    s2, p2 = o.patch_csr(int(ints[4]))
+    assert np.array_equal(s1, s2) and np.array_equal(p1, p2)
+    b1, q1 = c.block_csr()
+    b2, q2 = o.block_csr(int(ints[5]))
+    assert np.array_equal(b1, b2) and np.array_equal(q1, q2)
+
+
+@pytest.mark.parametrize("case,kernel", [("3d", 2), ("2d", 2), ("2d", 6), ("3d", 6), ("2d", 0 + 1)])
+def test_interpolation_fp64_matches_oracle(case, kernel):
+    xd, fd, xp, opts = small_3d() if case == "3d" else small_2d()
+    opts = dict(opts, kernel=kernel)
+    if kernel == 6:
+        opts["shape_factor"] = 3.0
+    c = gpu_ctx(opts)
+    o = Oracle(**opts)
+    c.fill_data(xd, fd)
+    c.fill_points(xp)
+    c.interpolate_c()
+    assert o.fill(True, xd, fd) == 0 and o.fill(False, xp) == 0 and o.interpolate() == 0
+    x1, f1, p1 = gpu_output(c, len(xp), opts["nfields"])
+    x2, f2, p2 = o.output(len(xp))
+    assert np.array_equal(p1, p2) and np.array_equal(x1, x2)
+    assert relerr(f1, f2) <= TOL64
+
+
+def test_weights_match_oracle():
+    xd, fd, xp, opts = small_3d()
+    c = gpu_ctx(opts)
+    o = Oracle(**opts)
+    c.fill_data(xd, fd)
+    c.fill_points(xp)
+    o.fill(True, xd, fd)
+    o.fill(False, xp)
+    _, w1, _ = gpu_output(c, len(xp), 8, "weights")
+    _, w2, _ = o.output(len(xp), "weights")
+    assert np.abs(w1 - w2).max() <= 1e-13
+
+
+@pytest.mark.parametrize("case", ["3d", "2d"])
+def test_fp32_eval_within_1e6_of_fp64(case):
+    xd, fd, xp, opts = small_3d(nlat=24, npu=6, np_=5000) if case == "3d" else small_2d()
+    res = {}
+    for prec in ("fp64", "fp32"):
+        c = gpu_ctx(opts, eval_precision=prec)
+        c.fill_data(xd, fd)
+        c.fill_points(xp)
+        c.interpolate_c()
+        res[prec] = gpu_output(c, len(xp), opts["nfields"])[1]
+    assert relerr(res["fp32"], res["fp64"]) <= TOL32
+
+
+@pytest.mark.parametrize("scheme", [0, 1, 2, 3])
+@pytest.mark.parametrize("solve_method", [2, 1])
+def test_advection_matches_oracle(scheme, solve_method):
+    xd, fd, xp, opts = small_3d(np_=2000)
+    adv = dict(advection=True, advection_scheme=scheme, advection_cfl=0.3, dt=1e-3, solve_method=solve_method)
+    c = gpu_ctx(opts, **adv)
+    o = Oracle(**opts, **adv)
+    t, dt = 0.0, 4e-3
+    for step in range(3):
+        c.fill_data(xd, fd)
+        assert o.fill(True, xd, fd) == 0
+        if step == 0:
+            c.fill_points(xp)
+            assert o.fill(False, xp) == 0
+        c.interpolate_c()
+        assert o.interpolate() == 0
+        c.advect_interpolate_c(t, t + dt)
+        assert o.advect(t, t + dt) == 0
+        t += dt
+    x1, f1, p1 = gpu_output(c, len(xp), 3)
+    x2, f2, p2 = o.output(len(xp))
+    assert np.array_equal(p1, p2)
+    assert np.abs(x1 - x2).max() <= 1e-12
+    assert relerr(f1, f2) <= TOL64
+    if scheme == 3:
+        assert abs(c.stats()["dt"] - o.dt()) <= 1e-12 * abs(o.dt())
+
+
+def test_particles_leaving_domain_are_dropped():
+    """A particle pushed out of [0,1]^3 is removed (DMSwarmMigrate on one rank); its output rows are 0."""
+    xd, fd, xp, opts = small_3d(np_=500)
+    fd = np.tile(np.array([[3.0, 0.0, 0.0]]), (len(xd), 1))  # uniform flow in +x
+    xp[:50, 0] = 0.999
+    adv = dict(advection=True, advection_scheme=2, advection_cfl=0.3)
+    c = gpu_ctx(opts, **adv)
+    o = Oracle(**opts, **adv)
+    c.fill_data(xd, fd); c.fill_points(xp); c.interpolate_c()
+    o.fill(True, xd, fd); o.fill(False, xp); o.interpolate()
+    c.advect_interpolate_c(0.0, 0.01)
+    o.advect(0.0, 0.01)
+    x1, f1, p1 = gpu_output(c, len(xp), 3)
+    x2, f2, p2 = o.output(len(xp))
+    assert np.array_equal(p1, p2)
+    assert (p1 == 0).sum() >= 50
+    assert np.abs(x1 - x2).max() <= 1e-12
+    assert c.stats()["np_alive"] == o.counts()[1]
+
+
+def test_lazy_setup_and_reset_semantics():
+    """Only patches touched by particles are set up; A_KSP_ASMB reset destroys them, A_KSP keeps them."""
+    xd, fd, xp, opts = small_3d(np_=20)
+    xp[:] = 0.1  # all particles in one cell
+    for sm, expect_after_reset in ((2, 0), (1, 8)):
+        c = gpu_ctx(opts, solve_method=sm)
+        o = Oracle(**opts, solve_method=sm)
+        c.fill_data(xd, fd); c.fill_points(xp); c.interpolate_c()
+        o.fill(True, xd, fd); o.fill(False, xp); o.interpolate()
+        assert c.stats()["npatch_setup"] == o.counts()[2] == 8
+        c.reset_coefficients(); o.reset()
+        assert c.stats()["npatch_setup"] == o.counts()[2] == expect_after_reset
+
+
+def test_analytical_advection_matches_oracle():
+    xd, fd, xp, opts = small_3d(np_=1000)
+    adv = dict(advection=True, advection_scheme=2, advection_cfl=0.3, nfields=0)
+    opts = dict(opts, nfields=0)
+
+    def rot(n, dim, x, v, user):
+        X = np.ctypeslib.as_array(x, shape=(n, dim))
+        V = np.ctypeslib.as_array(v, shape=(n, dim))
+        V[:, 0] = -(X[:, 1] - 0.5)
+        V[:, 1] = X[:, 0] - 0.5
+        V[:, 2] = 0.0
+        return 0
+
+    c = gpu_ctx(opts, **adv)
+    o = Oracle(**opts, **adv)
+    c.set_advection_function(rot)
+    o.set_velocity_batch(rot)
+    c.fill_points(xp)
+    o.fill(False, xp)
+    for s in range(3):
+        c.advect_analytical_c(s * 0.01, (s + 1) * 0.01)
+        assert o.advect_analytical(s * 0.01, (s + 1) * 0.01) == 0
+    x1, _, p1 = gpu_output(c, len(xp), 3, "velocity")
+    x2, _, p2 = o.output(len(xp), "velocity")
+    assert np.array_equal(p1, p2)
+    assert np.abs(x1 - x2).max() <= 1e-13
+
+
+def test_error_paths():
+    xd, fd, xp, opts = small_3d(np_=100)
+    c = gpu_ctx(opts)
+    bad = xp.copy()
+    bad[3, 1] = 1.5
+    with pytest.raises(RuntimeError, match="error code 62"):
+        c.fill_points(bad)
+    with pytest.raises(RuntimeError):
+        c.interpolate_c()
+    c.fill_data(xd, fd)
+    c.fill_points(xp)
+    c.interpolate_c()
+    x = np.zeros((10, 3))
+    with pytest.raises(RuntimeError, match="error code 63"):
+        c.output(coords=x)  # pids up to 100 do not fit 10 rows
+    # linear kernel: the collocation matrix is not positive definite -> zero-pivot error, no fault
+    c2 = gpu_ctx(opts, kernel=0)
+    c2.fill_data(xd, fd)
+    c2.fill_points(xp)
+    with pytest.raises(RuntimeError, match="error code 81"):
+        c2.interpolate_c()
+
+
+def test_interpolator_class_and_pid_roundtrip():
+    xd, fd, xp, opts = small_2d()
+    it = L.LagRBFInterpolator(**opts)
+    out = L.PointContainer.empty(len(xp), 2, 2)
+    it.interpolate(L.PointContainer(xd, fd), L.PointContainer(xp), out)
+    assert np.array_equal(out.pidx, np.arange(1, len(xp) + 1))
+    assert np.array_equal(out.coords, xp)
+    # second call with the returned pids: same values
+    out2 = L.PointContainer.empty(len(xp), 2, 2)
+    it.interpolate(L.PointContainer(xd, fd), L.PointContainer(xp, pidx=out.pidx[::-1].copy()), out2)
+    assert np.allclose(out2.values[::-1], out.values, rtol=0, atol=1e-12)
+
+
+def test_graph_and_eager_paths_agree():
+    xd, fd, xp, opts = small_3d(np_=1500)
+    adv = dict(advection=True, advection_scheme=2, advection_cfl=0.3)
+    outs = []
+    for graph in (True, False):
+        c = gpu_ctx(opts, use_cuda_graph=graph, **adv)
+        c.fill_data(xd, fd); c.fill_points(xp); c.interpolate_c()
+        c.advect_interpolate_c(0.0, 0.02)
+        outs.append(gpu_output(c, len(xp), 3))
+    assert np.array_equal(outs[0][0], outs[1][0]) and np.array_equal(outs[0][1], outs[1][1])
