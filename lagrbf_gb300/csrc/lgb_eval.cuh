@@ -183,69 +183,77 @@ __device__ __forceinline__ void eval_dispatch(int o, const Real *rec, int n, con
 #undef EV_CASE
 }
 
+/* Node-index range [lo, hi] along one axis that contains every node within the weight support of
+   coordinate x (conservative by one node on each side; phiW is exactly zero outside the support,
+   so extra candidates change nothing). */
+__device__ __forceinline__ void eval_node_range(double x, double O, double h, int n, double rad, int &lo, int &hi)
+{
+  const double ih = 1.0 / h;
+  int a = (int)floor((x - rad - O) * ih) - 1;
+  int b = (int)ceil((x + rad - O) * ih) + 1;
+  lo = (a < 0) ? 0 : a;
+  hi = (b > n - 1) ? n - 1 : b;
+}
+
 /* PU weights of one particle from the support nodes.  FP32: coordinates relative to the cell
-   origin, compensated sum.  FP64: absolute node coordinates as in the reference. */
+   origin (node ci, cj, cl), compensated sum.  FP64: absolute node coordinates as in the
+   reference.  pw[k] are the corner values phiW(|x - c_k|), den the sum over all nodes. */
 template <typename Real, int DIM>
 __device__ __forceinline__ void eval_weights(const lgb_geom &g, int ci, int cj, int cl, const double *x,
                                              const Real *xr, Real (&pw)[EGeo<DIM>::NEN], double &den, int &nsupp)
 {
   constexpr int NEN = EGeo<DIM>::NEN;
-  int cc[3] = {ci, cj, cl};
-  int lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
-  /* candidate nodes: a conservative float bound of the support box (phiW is exactly zero outside
-     the support, so extra candidates change nothing) */
-  const float rad = (float)(1.0 / g.eps_w);
-  for (int d = 0; d < DIM; d++) {
-    float rel = (float)(x[d] - (g.O[d] + g.h[d] * cc[d]));
-    float ih = (float)(1.0 / g.h[d]);
-    int a = (int)floorf((rel - rad) * ih) - 1, b = (int)ceilf((rel + rad) * ih) + 1;
-    a = max(a, -cc[d]); b = min(b, g.n[d] - 1 - cc[d]);
-    lo[d] = a; hi[d] = b;
-  }
+  const double rad = 1.0 / g.eps_w;
+  int ilo, ihi, jlo, jhi, klo = 0, khi = 0;
+  eval_node_range(x[0], g.O[0], g.h[0], g.n[0], rad, ilo, ihi);
+  eval_node_range(x[1], g.O[1], g.h[1], g.n[1], rad, jlo, jhi);
+  if constexpr (DIM == 3) eval_node_range(x[2], g.O[2], g.h[2], g.n[2], rad, klo, khi);
   nsupp = 0;
   if constexpr (sizeof(Real) == 4) {
-    float epsw = (float)g.eps_w, shi = 0.f, slo = 0.f;
-    float hf0 = (float)g.h[0], hf1 = (float)g.h[1], hf2 = (float)g.h[2];
-    for (int tz = lo[2]; tz <= hi[2]; tz++)
-      for (int ty = lo[1]; ty <= hi[1]; ty++)
-        for (int tx = lo[0]; tx <= hi[0]; tx++) {
-          float dx = xr[0] - tx * hf0, dy = xr[1] - ty * hf1, d2 = fmaf(dx, dx, dy * dy);
-          if constexpr (DIM == 3) { float dz = xr[2] - tz * hf2; d2 = fmaf(dz, dz, d2); }
-          float w = lgb_wendland_c2<float>(sqrtf(d2), epsw);
+    const float epsw = (float)g.eps_w, hf0 = (float)g.h[0], hf1 = (float)g.h[1], hf2 = (float)g.h[2];
+    float shi = 0.f, slo = 0.f;
+    for (int k = klo; k <= khi; k++) {
+      const float dz = (DIM == 3) ? xr[2] - (float)(k - cl) * hf2 : 0.f;
+      for (int j = jlo; j <= jhi; j++) {
+        const float dy = xr[1] - (float)(j - cj) * hf1;
+        for (int i = ilo; i <= ihi; i++) {
+          const float dx = xr[0] - (float)(i - ci) * hf0;
+          const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+          const float w = lgb_wendland_c2<float>(sqrtf(d2), epsw);
           nsupp += (w > 0.f);
           lgb_df_add(shi, slo, w);
         }
+      }
+    }
 #pragma unroll
-    for (int k = 0; k < NEN; k++) {
-      float dx = xr[0] - ecorner_ox(k) * hf0, dy = xr[1] - ecorner_oy(k) * hf1, d2 = fmaf(dx, dx, dy * dy);
-      if constexpr (DIM == 3) { float dz = xr[2] - ecorner_oz(DIM, k) * hf2; d2 = fmaf(dz, dz, d2); }
-      pw[k] = lgb_wendland_c2<float>(sqrtf(d2), epsw);
+    for (int q = 0; q < NEN; q++) {
+      float dx = xr[0] - ecorner_ox(q) * hf0, dy = xr[1] - ecorner_oy(q) * hf1;
+      float dz = (DIM == 3) ? xr[2] - ecorner_oz(DIM, q) * hf2 : 0.f;
+      pw[q] = lgb_wendland_c2<float>(sqrtf(fmaf(dx, dx, fmaf(dy, dy, dz * dz))), epsw);
     }
     den = (double)shi + (double)slo;
   } else {
     double sum = 0.0;
-    for (int tz = lo[2]; tz <= hi[2]; tz++)
-      for (int ty = lo[1]; ty <= hi[1]; ty++)
-        for (int tx = lo[0]; tx <= hi[0]; tx++) {
-          double dx = x[0] - (g.O[0] + g.h[0] * (ci + tx));
-          double dy = x[1] - (g.O[1] + g.h[1] * (cj + ty)), d2;
-          if constexpr (DIM == 3) {
-            double dz = x[2] - (g.O[2] + g.h[2] * (cl + tz));
-            d2 = fma(dx, dx, fma(dy, dy, dz * dz));
-          } else d2 = fma(dx, dx, dy * dy);
-          double w = lgb_wendland_c2<double>(sqrt(d2), g.eps_w);
+    for (int k = klo; k <= khi; k++) {
+      const double dz = (DIM == 3) ? x[2] - (g.O[2] + g.h[2] * k) : 0.0;
+      for (int j = jlo; j <= jhi; j++) {
+        const double dy = x[1] - (g.O[1] + g.h[1] * j);
+        for (int i = ilo; i <= ihi; i++) {
+          const double dx = x[0] - (g.O[0] + g.h[0] * i);
+          const double d2 = (DIM == 3) ? fma(dx, dx, fma(dy, dy, dz * dz)) : fma(dx, dx, dy * dy);
+          const double w = lgb_wendland_c2<double>(sqrt(d2), g.eps_w);
           nsupp += (w > 0.0);
           sum += w;
         }
+      }
+    }
 #pragma unroll
-    for (int k = 0; k < NEN; k++) {
-      double dx = x[0] - (g.O[0] + g.h[0] * (ci + ecorner_ox(k)));
-      double dy = x[1] - (g.O[1] + g.h[1] * (cj + ecorner_oy(k))), d2;
-      if constexpr (DIM == 3) {
-        double dz = x[2] - (g.O[2] + g.h[2] * (cl + ecorner_oz(DIM, k)));
-        d2 = fma(dx, dx, fma(dy, dy, dz * dz));
-      } else d2 = fma(dx, dx, dy * dy);
-      pw[k] = (Real)lgb_wendland_c2<double>(sqrt(d2), g.eps_w);
+    for (int q = 0; q < NEN; q++) {
+      const double dx = x[0] - (g.O[0] + g.h[0] * (ci + ecorner_ox(q)));
+      const double dy = x[1] - (g.O[1] + g.h[1] * (cj + ecorner_oy(q)));
+      const double dz = (DIM == 3) ? x[2] - (g.O[2] + g.h[2] * (cl + ecorner_oz(DIM, q))) : 0.0;
+      const double d2 = (DIM == 3) ? fma(dx, dx, fma(dy, dy, dz * dz)) : fma(dx, dx, dy * dy);
+      pw[q] = (Real)lgb_wendland_c2<double>(sqrt(d2), g.eps_w);
     }
     den = sum;
   }

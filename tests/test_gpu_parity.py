@@ -85,7 +85,11 @@ def test_interpolation_fp64_matches_oracle(case, kernel):
     xd, fd, xp, opts = small_3d() if case == "3d" else small_2d()
     opts = dict(opts, kernel=kernel)
     if kernel == 6:
-        opts["shape_factor"] = 3.0
+        # Gaussian with eps_r = 3/h (h = lattice spacing), the 2D benchmark's choice: well conditioned
+        nlat = 20 if case == "3d" else 32
+        n = opts["npartitions"][0]
+        eps_w = n / opts["overlap"]
+        opts["shape_factor"] = 3.0 * nlat / eps_w
     c = gpu_ctx(opts)
     o = Oracle(**opts)
     c.fill_data(xd, fd)
@@ -188,7 +192,7 @@ def test_lazy_setup_and_reset_semantics():
 
 def test_analytical_advection_matches_oracle():
     xd, fd, xp, opts = small_3d(np_=1000)
-    adv = dict(advection=True, advection_scheme=2, advection_cfl=0.3, nfields=0)
+    adv = dict(advection=True, advection_scheme=2, advection_cfl=0.3)
     opts = dict(opts, nfields=0)
 
     def rot(n, dim, x, v, user):
