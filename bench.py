@@ -1,0 +1,350 @@
+"""Benchmark: 3D RK4 RBF-PU advection throughput (particle-steps/s) on GB300.
+
+Workload (default): 2,097,152 source nodes on a 128^3 jittered lattice in [0,1]^3 carrying the ABC
+flow (A=B=C=1, X = 2 pi x), 32^3 PU patches (overlap 1.5 x spacing), Wendland C2 kernel, 16,777,216
+uniform particles, RK4 with dt = 5e-4.  One step = one internal RK4 step of the reference's
+interpolated advection loop over [t, t+dt] (3 stage evaluations + the "fields" evaluation, 4 particle
+re-binnings, lazy patch set-up check, CFL reduction).  Inputs are seeded synthetic data (no dataset).
+
+Legs:
+  value      FP32-evaluation path, data/binning/factors resident in HBM (lagrbf_gpu_advect_resident)
+  fp64       the plain FP64 path on the same context, and the FP32-vs-FP64 error after one step
+  e2e        through the reference-facing C-ABI with host buffers, per step: fill_swarm(data),
+             lagrbf_interpolation, lagrbf_output(coords, fields, pids), lagrbf_advect_interpolate
+             (A_KSP: factors kept, coefficients re-solved each step, as the reference's reset implies)
+  roofline   the evaluation kernel: algorithmic flops (counted on the device) / event-timed duration
+  cpu_baseline / --impl reference: the reference algorithm on the host cores (oracle/cpu_baseline.py)
+
+Run: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference] [--np NP]
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "3D RK4 particle-steps/s (FP32 eval <=1e-6 vs FP64; plain FP64 alongside)"
+DT = 5e-4
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--np", type=int, default=16_777_216, help="particles per GPU")
+    ap.add_argument("--nlat", type=int, default=128)
+    ap.add_argument("--npu", type=int, default=32)
+    ap.add_argument("--fp64-steps", type=int, default=2)
+    ap.add_argument("--e2e-steps", type=int, default=0, help="0: same as --steps")
+    ap.add_argument("--cpu-sample", type=int, default=256, help="particles per emulated rank")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--profile-only", action="store_true", help="setup + a few steps, for ncu")
+    return ap.parse_args()
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    def __init__(self, gpu=0):
+        self.gpu = gpu
+        self.samples = []
+        self.proc = None
+
+    def start(self):
+        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.th = threading.Thread(target=self._read, daemon=True)
+            self.th.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.samples.append([x.strip() for x in line.split(",")])
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples for i in range(4) if len(s) > 3 + i and "Active" in s[3 + i]
+                          and "Not" not in s[3 + i]})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            return json.load(f), "measured"
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+def workload(args, rank):
+    from lagrbf_gb300 import workloads as W
+    xd, fd, xp, opts = W.config_abc_3d(nlat=args.nlat, npu=args.npu, np_=args.np, seed=3)
+    if rank:
+        xp = W.uniform_points(args.np, 3, np.random.default_rng(4 + 1000 * rank))
+    return xd, fd, xp, opts
+
+
+def cpu_baseline(xd, fd, opts, args, nsteps=1):
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import cpu_baseline as CB
+    P = os.cpu_count() or 1
+    r = CB.time_reference(xd, fd, args.npu, dict(opts, advection_scheme=2), P, args.cpu_sample, nsteps, DT)
+    return r, P
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    xd, fd, _, opts = workload(args, 0)
+    total_ps, total_s = 0, 0.0
+    for _ in range(args.warmup if args.warmup < 2 else 1):
+        cpu_baseline(xd, fd, opts, args, 1)
+    for _ in range(args.steps):
+        r, P = cpu_baseline(xd, fd, opts, args, 1)
+        total_ps += r["particle_steps"]
+        total_s += r["step_s"]
+    v = total_ps / total_s
+    sample = ("%d emulated MPI ranks (DMDA split of the 32^3 PU mesh, one-cell halo, rank-local data) x %d "
+              "particles each, 1 RK4 step per bench step; oracle port compiled with the reference's flags"
+              % (P, args.cpu_sample))
+    line = {"metric": METRIC, "value": v, "unit": "particle-steps/s", "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * total_s / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "impl": "reference",
+            "config": {"workload": "abc3d: 128^3 lattice, ABC flow, 32^3 PU, Wendland C2, RK4 dt=5e-4",
+                       "particles_per_rank_sample": args.cpu_sample, "ranks": P},
+            "cpu_baseline": {"value": v, "unit": "particle-steps/s", "cores": P, "kind": "port", "sample": sample},
+            "e2e": {"value": v, "unit": "particle-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+def relerr_stats(a, b):
+    den = np.abs(b).max(axis=0)
+    den[den == 0] = 1.0
+    mx = (np.abs(a - b).max(axis=0) / den)
+    rms = np.sqrt(((a - b) ** 2).mean(axis=0)) / np.maximum(np.sqrt((b ** 2).mean(axis=0)), 1e-300)
+    return [float(x) for x in mx], [float(x) for x in rms]
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch
+        import torch.distributed as tdist
+        torch.cuda.set_device(local)
+        tdist.init_process_group("nccl")
+        dist = tdist
+
+    def barrier():
+        if dist:
+            dist.barrier()
+
+    def allmax(x):
+        if not dist:
+            return x
+        import torch
+        t = torch.tensor([x], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    def allsum(x):
+        if not dist:
+            return x
+        import torch
+        t = torch.tensor([x], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.SUM)
+        return float(t.item())
+
+    import lagrbf_gb300 as L
+    cf = L.load_cfuncs()
+    xd, fd, xp, opts = workload(args, rank)
+    npart = len(xp)
+    ctx = L.LagRBFCtx(**opts, advection=True, advection_scheme=2, advection_cfl=0.3, dt=DT, solve_method=1,
+                      eval_precision="fp32", cuda_device=local)
+    # ---------------- setup (not timed in `value`) ----------------
+    t0 = time.perf_counter()
+    ctx.fill_data(xd, fd)
+    ctx.fill_points(xp)
+    ctx.interpolate_c()
+    ctx.synchronize()
+    setup_s = time.perf_counter() - t0
+    st0 = ctx.stats()
+    if args.profile_only:
+        for s in range(max(args.steps, 1)):
+            ctx.advect_resident(s * DT, (s + 1) * DT)
+        ctx.synchronize()
+        print(json.dumps({"profile_only": True, "setup_s": setup_s, "stats": ctx.stats()}))
+        return 0
+    t = 0.0
+    for _ in range(args.warmup):
+        ctx.advect_resident(t, t + DT)
+        t += DT
+    ctx.synchronize()
+    # ---------------- timed FP32 loop ----------------
+    ctx.reset_stats()
+    clocks = ClockSampler(local)
+    clocks.start()
+    barrier()
+    ctx.synchronize()
+    ts = time.perf_counter()
+    for _ in range(args.steps):
+        ctx.advect_resident(t, t + DT)
+        t += DT
+    ctx.synchronize()
+    barrier()
+    el = time.perf_counter() - ts
+    clk = clocks.stop()
+    st = ctx.stats()
+    el_max = allmax(el)
+    ps_total = allsum(st["particle_steps"])
+    value = ps_total / el_max
+    launches = st["launches"]
+    # ---------------- roofline of the evaluation kernel (event-timed launches) ----------------
+    ctx.reset_stats()
+    ctx.set_profiling(True)
+    nprof = min(3, args.steps)
+    for _ in range(nprof):
+        ctx.advect_resident(t, t + DT)
+        t += DT
+    ctx.synchronize()
+    sp = ctx.stats()
+    ctx.set_profiling(False)
+    pk, pk_kind = peaks()
+    fp32_peak = cf["lagrbf_gpu_fp32_peak_tflops"]()
+    eval_tflops = sp["eval_flops"] / (sp["eval_ms"] * 1e-3) / 1e12 if sp["eval_ms"] > 0 else 0.0
+    eval_gbs = sp["eval_bytes"] / (sp["eval_ms"] * 1e-3) / 1e9 if sp["eval_ms"] > 0 else 0.0
+    roofline = {"bound": "fp32", "achieved": eval_tflops, "peak": fp32_peak, "unit": "TFLOP/s",
+                "frac": eval_tflops / fp32_peak if fp32_peak > 0 else None, "traffic": None,
+                "kernel": "k_eval<float,3,3,2,KER_C2> (PU evaluation)",
+                "peak_source": "measured: FFMA-chain probe on this GPU in this run (lagrbf_gpu_fp32_peak_tflops)",
+                "per_launch_ms": sp["eval_ms"] / max(sp["eval_launches"], 1),
+                "flops_per_launch": sp["eval_flops"] / max(sp["eval_launches"], 1),
+                "bytes_per_launch": sp["eval_bytes"] / max(sp["eval_launches"], 1),
+                "hbm_achieved_gbs": eval_gbs, "hbm_peak_gbs": pk.get("hbm_gbs"),
+                "hbm_frac": eval_gbs / pk["hbm_gbs"] if pk.get("hbm_gbs") else None, "hbm_peak_kind": pk_kind,
+                "eval_share_of_step": (sp["eval_ms"] / nprof) / (1e3 * el / args.steps)}
+    # ---------------- FP32 vs FP64 error after one step from the same state ----------------
+    def snapshot():
+        x = np.zeros((npart, 3)); f = np.zeros((npart, 3)); p = np.zeros(npart, dtype=np.int64)
+        ctx.output(coords=x, fvals=f, pidx=p)
+        return x, f, p
+
+    x_start, f_start, p_start = snapshot()
+    alive = p_start > 0
+    ctx.set_precision(False)
+    ctx.fill_points(x_start[alive], values=f_start[alive], pidx=p_start[alive])
+    ctx.advect_resident(t, t + DT)
+    x64, f64, _ = snapshot()
+    ctx.set_precision(True)
+    ctx.fill_points(x_start[alive], values=f_start[alive], pidx=p_start[alive])
+    ctx.advect_resident(t, t + DT)
+    x32, f32, _ = snapshot()
+    err_max, err_rms = relerr_stats(f32, f64)
+    pos_err = float(np.abs(x32 - x64).max())
+    # ---------------- plain FP64 path throughput ----------------
+    ctx.set_precision(False)
+    ctx.reset_stats()
+    ctx.synchronize()
+    ts = time.perf_counter()
+    for _ in range(args.fp64_steps):
+        ctx.advect_resident(t, t + DT)
+        t += DT
+    ctx.synchronize()
+    el64 = allmax(time.perf_counter() - ts)
+    value64 = allsum(ctx.stats()["particle_steps"]) / el64
+    ctx.set_precision(True)
+    # ---------------- end to end through the reference-facing C-ABI, host buffers ----------------
+    ke = args.e2e_steps or args.steps
+    xo = np.zeros((npart, 3)); fo = np.zeros((npart, 3)); po = np.zeros(npart, dtype=np.int64)
+    ctx.fill_points(x_start[alive], values=f_start[alive], pidx=p_start[alive])
+    h2d = xd.nbytes + fd.nbytes
+    d2h = xo.nbytes + fo.nbytes + po.nbytes
+    ctx.reset_stats()
+    barrier()
+    ts = time.perf_counter()
+    for _ in range(ke):
+        ctx.fill_data(xd, fd)
+        ctx.interpolate_c()
+        ctx.output(coords=xo, fvals=fo, pidx=po)
+        ctx.advect_interpolate_c(t, t + DT)
+        t += DT
+    ctx.synchronize()
+    barrier()
+    ele = allmax(time.perf_counter() - ts)
+    e2e = allsum(ctx.stats()["particle_steps"]) / ele
+    # ---------------- CPU baseline on the host cores ----------------
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        try:
+            r, P = cpu_baseline(xd, fd, opts, args, 1)
+            cpu = {"value": r["particle_steps"] / r["step_s"], "unit": "particle-steps/s", "cores": P, "kind": "port",
+                   "sample": "%d emulated MPI ranks x %d particles, 1 RK4 step, rank-local data (~%d points) and "
+                             "patches; oracle port with the reference's compiler flags" % (P, args.cpu_sample,
+                                                                                            r["local_data"])}
+        except Exception as e:  # the baseline is reported, not required
+            cpu = {"value": None, "error": str(e)[:200]}
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "particle-steps/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * el_max / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "abc3d: %d^3 jittered lattice (%d nodes), ABC flow, %d^3 PU patches, Wendland C2, "
+                                   "%d particles/GPU, RK4 dt=%g" % (args.nlat, len(xd), args.npu, args.np, DT),
+                       "eval": "FP32 evaluation, FP64 factorisation and weight normalisation",
+                       "solve_method": "A_KSP (factors resident)",
+                       "l2": "inputs larger than L2 (particle state %.1f GB)" % (npart * 8 * 3 * 12 / 1e9),
+                       "parallelism": "replicas x%d (particles sharded, data replicated)" % world,
+                       "setup_s": setup_s, "patches_factored": st0["patches_factored"],
+                       "max_patch": st0["max_patch"]},
+            "fp64": {"value": value64, "unit": "particle-steps/s", "steps": args.fp64_steps,
+                     "fp32_speedup": value / value64 if value64 > 0 else None,
+                     "fp32_vs_fp64_max_rel_err": err_max, "fp32_vs_fp64_rms_rel_err": err_rms,
+                     "fp32_vs_fp64_max_abs_pos_err": pos_err,
+                     "err_definition": "per component: max_p|a-b| / max_p|b| and RMS(a-b)/RMS(b), fields after 1 step"},
+            "e2e": {"value": e2e, "unit": "particle-steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                    "steps": ke, "path": "fill_swarm(data) + lagrbf_interpolation + lagrbf_output + "
+                                         "lagrbf_advect_interpolate, host numpy buffers"},
+            "roofline": roofline, "cpu_baseline": cpu, "clocks": clk, "gpu_launches": launches,
+        }
+        print(json.dumps(line))
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

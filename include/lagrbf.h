@@ -90,7 +90,8 @@ LAGRBF_EXPORT void lagrbf_interpolate_driver(int32_t ndata_local, double *data_c
    pu_mesh_shape_factor, n_interpolation_fields, kernel_type, solve_method, advection,
    advection_scheme, velocity_name, dt, cfl_fac, rmin, rmax, dopri_dt_fac, dopri_dt_fac_min,
    dopri_dt_fac_max, dopri_atol, dopri_rtol; and the GPU-only keys eval_precision (fp64|fp32,
-   default fp64), use_cuda_graph (bool, default true).  Arrays are comma separated. */
+   default fp64), use_cuda_graph (bool, default true), cuda_device (int).  Arrays are comma
+   separated. */
 LAGRBF_EXPORT int lagrbf_options_set_value(const char *name, const char *value);
 LAGRBF_EXPORT int lagrbf_options_clear(void);
 LAGRBF_EXPORT int lagrbf_options_insert_file(const char *path);
@@ -118,6 +119,14 @@ typedef struct {
   double  dt;                 /* the advection context's current time step                   */
 } lagrbf_stats_t;
 
+/* The interpolated advection loop of lagrbf_advect_interpolate over [time, time_next] without its
+   end-of-call reset: the data swarm, binning and patch set-ups stay resident for the next call. */
+LAGRBF_EXPORT int lagrbf_gpu_advect_resident(void *ctx, double time, double time_next);
+/* Switches the evaluation precision of a live context (1: FP32 evaluation, 0: FP64). */
+LAGRBF_EXPORT int lagrbf_gpu_set_precision(void *ctx, int fp32);
+/* FP32 FMA throughput of the current device in TFLOP/s, measured by a synthetic kernel
+   (dependent FFMA chains, all SMs): the FP32 roofline denominator. */
+LAGRBF_EXPORT double lagrbf_gpu_fp32_peak_tflops(void);
 /* Kernel-level event timing of the evaluation and factorisation launches (disables graph
    capture while on, so every launch is bracketed by events on the context's stream). */
 LAGRBF_EXPORT int lagrbf_gpu_set_profiling(void *ctx, int on);

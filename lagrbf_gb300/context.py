@@ -84,6 +84,8 @@ class LagRBFCtx:
         o["rmax"] = kwargs.get("rmax", o.getReal("rmax", 1e132))
         o["eval_precision"] = kwargs.get("eval_precision", o.getString("eval_precision", "fp64"))
         o["use_cuda_graph"] = kwargs.get("use_cuda_graph", o.getBool("use_cuda_graph", True))
+        if "cuda_device" in kwargs or "cuda_device" in o:
+            o["cuda_device"] = int(kwargs.get("cuda_device", o.get("cuda_device", 0)))
         self.nfields = int(o["n_interpolation_fields"])
         self._cf = load_cfuncs()
         self._cf["lagrbf_options_clear"]()
@@ -223,6 +225,15 @@ class LagRBFCtx:
 
     def set_profiling(self, on):
         self._check(self._cf["lagrbf_gpu_set_profiling"](self.ctx, int(bool(on))), "lagrbf_gpu_set_profiling")
+
+    def advect_resident(self, time_start, time_end):
+        """The advection loop of advect_interpolate_c without its end-of-call reset (data, binning
+        and patch set-ups stay resident)."""
+        self._check(self._cf["lagrbf_gpu_advect_resident"](self.ctx, float(time_start), float(time_end)),
+                    "lagrbf_gpu_advect_resident")
+
+    def set_precision(self, fp32):
+        self._check(self._cf["lagrbf_gpu_set_precision"](self.ctx, int(bool(fp32))), "lagrbf_gpu_set_precision")
 
     def synchronize(self):
         self._check(self._cf["lagrbf_gpu_synchronize"](self.ctx), "lagrbf_gpu_synchronize")

@@ -226,7 +226,7 @@ typedef struct {
   /* graph of one internal step */
   cudaGraphExec_t graph;
   int graph_valid;
-  long long graph_launches;
+  long long graph_launches, graph_eval_launches;
   /* pinned control copy */
   lgb_ctrl *hctrl;
   /* profiling */
@@ -389,6 +389,13 @@ static int create_ctx(lgb_ctx **out)
   if (!c) return set_error(LAGRBF_ERR_MEM, "out of host memory");
   d = &c->d;
   if ((i = read_options(c))) { free(c); return i; }
+  {
+    int dev = -1;
+    if (opt_int("cuda_device", &dev) && dev >= 0 && cudaSetDevice(dev) != cudaSuccess) {
+      free(c);
+      return set_error(LAGRBF_ERR_GPU, "cudaSetDevice(%d) failed", dev);
+    }
+  }
   if (lgb_device_info(&d->nsm, &d->smem_optin)) { free(c); return set_error(LAGRBF_ERR_GPU, "no CUDA device"); }
   if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
     free(c);
@@ -813,15 +820,18 @@ static int run_step(lgb_ctx *c, int analytical)
   } else if (c->graph_valid) {
     CU(cudaGraphLaunch(c->graph, c->stream));
     c->launches_graph += c->graph_launches;
+    c->eval_launches += c->graph_eval_launches;
   } else {
     cudaGraph_t graph;
-    long long l0 = lgb_launch_count();
+    long long l0 = lgb_launch_count(), e0 = c->eval_launches;
     cudaError_t e = cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal);
     int rc = 0;
     if (e == cudaSuccess) {
       rc = step_sequence(c, 0);
       e = cudaStreamEndCapture(c->stream, &graph);
     }
+    c->graph_eval_launches = c->eval_launches - e0;
+    c->eval_launches = e0;
     if (e != cudaSuccess || rc) {
       /* capture not possible: run this step eagerly and stop using graphs */
       cudaGetLastError();
@@ -841,6 +851,7 @@ static int run_step(lgb_ctx *c, int analytical)
         c->launch_base += c->graph_launches;
         CU(cudaGraphLaunch(c->graph, c->stream));
         c->launches_graph += c->graph_launches;
+        c->eval_launches += c->graph_eval_launches;
       }
     }
   }
@@ -850,7 +861,7 @@ static int run_step(lgb_ctx *c, int analytical)
   return 0;
 }
 
-static int advection_loop(lgb_ctx *c, double t, double t_next, int analytical)
+static int advection_loop(lgb_ctx *c, double t, double t_next, int analytical, int keep)
 {
   lgb_dev *d = &c->d;
   int it = 0;
@@ -879,7 +890,7 @@ static int advection_loop(lgb_ctx *c, double t, double t_next, int analytical)
     t = c->hctrl->t;
     it++;
   }
-  if (!analytical) {
+  if (!analytical && !keep) {
     /* end of the time step (time_loop.c:93-98): reset partitions, cell info, clear the data swarm */
     TRY(reset_coefficients(c));
     c->data_filled = 0;
@@ -1031,7 +1042,7 @@ LAGRBF_EXPORT int lagrbf_avect_analytical(void *ctx, double time, double time_ne
   lgb_ctx *c = (lgb_ctx *)ctx;
   if (!c) return set_error(LAGRBF_ERR_ARG_NULL, "LagRBFCtx is NULL");
   if (!c->vfn && !c->vfnb) return set_error(LAGRBF_ERR_ARG_NULL, "no velocity function registered");
-  return advection_loop(c, time, time_next, 1);
+  return advection_loop(c, time, time_next, 1, 0);
 }
 
 LAGRBF_EXPORT int lagrbf_advect_interpolate(void *ctx, double time, double time_next)
@@ -1039,7 +1050,7 @@ LAGRBF_EXPORT int lagrbf_advect_interpolate(void *ctx, double time, double time_
   lgb_ctx *c = (lgb_ctx *)ctx;
   if (!c) return set_error(LAGRBF_ERR_ARG_NULL, "LagRBFCtx is NULL");
   if (c->vfn || c->vfnb) return set_error(LAGRBF_ERR_ARG_WRONGSTATE, "an analytical velocity function is registered");
-  return advection_loop(c, time, time_next, 0);
+  return advection_loop(c, time, time_next, 0, 0);
 }
 
 LAGRBF_EXPORT int lagrbf_advection_function(void *ctx, int (*velocity_fn)(double *, double *, void *), void *fn_ctx)
@@ -1081,11 +1092,33 @@ LAGRBF_EXPORT void lagrbf_interpolate_driver(int32_t ndata_local, double *data_c
 /* ======================================================================================= */
 /* section 3: GPU-level extension                                                           */
 /* ======================================================================================= */
+LAGRBF_EXPORT int lagrbf_gpu_advect_resident(void *ctx, double time, double time_next)
+{
+  lgb_ctx *c = (lgb_ctx *)ctx;
+  if (!c) return set_error(LAGRBF_ERR_ARG_NULL, "LagRBFCtx is NULL");
+  if (c->vfn || c->vfnb) return set_error(LAGRBF_ERR_ARG_WRONGSTATE, "an analytical velocity function is registered");
+  return advection_loop(c, time, time_next, 0, 1);
+}
+
+double lgb_fp32_peak_tflops(void);
+LAGRBF_EXPORT double lagrbf_gpu_fp32_peak_tflops(void) { return lgb_fp32_peak_tflops(); }
+
+LAGRBF_EXPORT int lagrbf_gpu_set_precision(void *ctx, int fp32)
+{
+  lgb_ctx *c = (lgb_ctx *)ctx;
+  if (!c) return set_error(LAGRBF_ERR_ARG_NULL, "context is NULL");
+  CU(cudaStreamSynchronize(c->stream));
+  c->d.prec = fp32 ? LGB_PREC_FP32 : LGB_PREC_FP64;
+  invalidate_graph(c);
+  return 0;
+}
+
 LAGRBF_EXPORT int lagrbf_gpu_set_profiling(void *ctx, int on)
 {
   lgb_ctx *c = (lgb_ctx *)ctx;
   if (!c) return set_error(LAGRBF_ERR_ARG_NULL, "context is NULL");
   c->profiling = on ? 1 : 0;
+  if (on) invalidate_graph(c);
   return 0;
 }
 

@@ -496,6 +496,20 @@ static void eval_one(const orc_pu *pu, int kernel, const double *x, int cell, co
   }
 }
 
+static void eval_all(const orc_pu *pu, int kernel, int np, const double *xp, const int *cellid, const int *alive,
+                     const double *weights, const double *xd, const int *blk_start, const int *blk_pts,
+                     const int *patch_start, const int *patch_pts, const int *patch_setup, double *const *coeffs,
+                     int nf, double *values, double *rbf_d)
+{
+  int p;
+  for (p = 0; p < np; p++) {
+    if (alive && !alive[p]) continue;
+    if (cellid[p] < 0) continue;
+    eval_one(pu, kernel, &xp[pu->dim * p], cellid[p], &weights[pu->nen * p], xd, blk_start, blk_pts,
+             patch_start, patch_pts, patch_setup, coeffs, nf, rbf_d, &values[(size_t)nf * p]);
+  }
+}
+
 void orc_eval(const orc_pu *pu, int kernel, int np, const double *xp, const int *cellid, const int *alive,
               const double *weights, const double *xd, const int *blk_start, const int *blk_pts,
               const int *patch_start, const int *patch_pts, const int *patch_setup, double *const *coeffs,
@@ -758,8 +772,12 @@ static void rbf_interpolation(orc_ctx *c, int nf, double *values)
     if (c->patch_setup[node] && c->patch_m[node])
       memcpy(&pp[ps[node]], c->patch_idx[node], sizeof(int) * (size_t)c->patch_m[node]);
   }
-  orc_eval(&c->pu, c->cfg.kernel, c->np, c->xp, c->cell_p, c->alive, c->weights, c->xd, c->blk_start,
-           c->blk_pts, ps, pp, setup, cf, nf, values);
+  {
+    double *rbf_d = (double *)calloc((size_t)c->nd + 1, sizeof(double));
+    eval_all(&c->pu, c->cfg.kernel, c->np, c->xp, c->cell_p, c->alive, c->weights, c->xd, c->blk_start,
+             c->blk_pts, ps, pp, setup, cf, nf, values, rbf_d);
+    free(rbf_d);
+  }
   free(ps); free(pp); free(setup); free(cf);
 }
 
@@ -1165,5 +1183,48 @@ int orc_time_baseline(const orc_config *cfg, int nd, const double *xd, const dou
   free(ctxs);
   if (setup_s) *setup_s = t1 - t0;
   if (step_s) *step_s = t2 - t1;
+  return err;
+}
+
+int orc_time_ranks(int nranks, const orc_config *cfgs, const int *nd, const double *const *xd,
+                   const double *const *fd, const int *np, const double *const *xp, int nsteps, double dt,
+                   double *setup_s, double *step_s, long *psteps)
+{
+  int err = 0, r;
+  long ps = 0;
+  double t0, t1, t2;
+  orc_ctx **ctxs = (orc_ctx **)calloc((size_t)nranks, sizeof(orc_ctx *));
+  t0 = now_s();
+#pragma omp parallel for num_threads(nranks) schedule(static, 1) reduction(| : err)
+  for (r = 0; r < nranks; r++) {
+    orc_ctx *c = orc_create(&cfgs[r]);
+    int e;
+    ctxs[r] = c;
+    if (!c) { err |= 1; continue; }
+    e = orc_fill_swarm(c, 1, nd[r], xd[r], fd[r], NULL);
+    if (!e) e = orc_fill_swarm(c, 0, np[r], xp[r], NULL, NULL);
+    if (!e) e = orc_interpolation(c);
+    err |= e;
+  }
+  t1 = now_s();
+#pragma omp parallel for num_threads(nranks) schedule(static, 1) reduction(| : err) reduction(+ : ps)
+  for (r = 0; r < nranks; r++) {
+    orc_ctx *c = ctxs[r];
+    int s, e = 0, p;
+    double t = 0.0;
+    if (!c) continue;
+    for (s = 0; s < nsteps && !e; s++) {
+      e = advection_loop(c, t, t + dt, 1, 1);
+      t += dt;
+      for (p = 0; p < c->np; p++) ps += c->alive[p];
+    }
+    err |= e;
+  }
+  t2 = now_s();
+  for (r = 0; r < nranks; r++) orc_destroy(ctxs[r]);
+  free(ctxs);
+  if (setup_s) *setup_s = t1 - t0;
+  if (step_s) *step_s = t2 - t1;
+  if (psteps) *psteps = ps;
   return err;
 }

@@ -127,6 +127,13 @@ int      orc_time_baseline(const orc_config *cfg, int nd, const double *xd, cons
                            const double *xp, int nsteps, double dt, int nthreads, double *setup_s,
                            double *step_s);
 
+/* Emulated MPI ranks, each its own sub-problem (local PU sub-mesh with halo, the data of its
+   local box, a particle sample): one OpenMP thread per rank, setup then `nsteps` steady-state
+   advection steps of [t, t+dt].  Returns live particle-steps advanced in *psteps. */
+int      orc_time_ranks(int nranks, const orc_config *cfgs, const int *nd, const double *const *xd,
+                        const double *const *fd, const int *np, const double *const *xp, int nsteps, double dt,
+                        double *setup_s, double *step_s, long *psteps);
+
 #ifdef __cplusplus
 }
 #endif
