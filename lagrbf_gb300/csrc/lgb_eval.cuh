@@ -110,7 +110,8 @@ __device__ __forceinline__ Real eval_phi(Real d2, Real eps, Real ga, int kernel)
 /* Accumulate one staged segment of neighbour offset O. */
 template <typename Real, int DIM, int FP, int R, int KER, int O>
 __device__ __forceinline__ void eval_segment(const Real *__restrict__ rec, int n, const Real (&px)[R][3],
-                                             Real (&acc)[R][EGeo<DIM>::NEN][FP], Real eps, Real ga, int kernel)
+                                             Real (&acc)[R][EGeo<DIM>::NEN][FP], Real eps, Real ga, int kernel,
+                                             float *__restrict__ run, int rstride)
 {
   constexpr int NEN = EGeo<DIM>::NEN;
   constexpr int MASK = einv_mask(DIM, O);
@@ -119,7 +120,7 @@ __device__ __forceinline__ void eval_segment(const Real *__restrict__ rec, int n
   using V = typename std::conditional<sizeof(Real) == 4, float4, double2>::type;
   constexpr int VW = sizeof(V) / sizeof(Real);
   constexpr int NV = S / VW;
-#pragma unroll 2
+#pragma unroll 1
   for (int p = 0; p < n; ++p) {
     Real v[S];
     const V *rv = reinterpret_cast<const V *>(rec + (size_t)p * S);
@@ -159,13 +160,32 @@ __device__ __forceinline__ void eval_segment(const Real *__restrict__ rec, int n
       }
     }
   }
+  if constexpr (sizeof(Real) == 4) {
+    /* blocked summation: the segment's partial sums (one neighbour cell, <= budget points) go into
+       per-thread running sums in shared memory, which bounds the FP32 accumulation error by the
+       segment length instead of the patch size */
+#pragma unroll
+    for (int k = 0; k < NEN; k++) {
+      if ((MASK >> k) & 1) {
+#pragma unroll
+        for (int f = 0; f < FP; f++)
+#pragma unroll
+          for (int r = 0; r < R; r++) {
+            float *q = run + (size_t)(k * FP + f) * rstride + r * (rstride / R);
+            *q += acc[r][k][f];
+            acc[r][k][f] = 0.f;
+          }
+      }
+    }
+  }
 }
 
 template <typename Real, int DIM, int FP, int R, int KER>
 __device__ __forceinline__ void eval_dispatch(int o, const Real *rec, int n, const Real (&px)[R][3],
-                                              Real (&acc)[R][EGeo<DIM>::NEN][FP], Real eps, Real ga, int kernel)
+                                              Real (&acc)[R][EGeo<DIM>::NEN][FP], Real eps, Real ga, int kernel,
+                                              float *run, int rstride)
 {
-#define EV_CASE(OO) case OO: eval_segment<Real, DIM, FP, R, KER, OO>(rec, n, px, acc, eps, ga, kernel); break;
+#define EV_CASE(OO) case OO: eval_segment<Real, DIM, FP, R, KER, OO>(rec, n, px, acc, eps, ga, kernel, run, rstride); break;
   if constexpr (DIM == 3) {
     switch (o) {
       EV_CASE(0) EV_CASE(1) EV_CASE(2) EV_CASE(3) EV_CASE(4) EV_CASE(5) EV_CASE(6) EV_CASE(7) EV_CASE(8)
@@ -282,10 +302,13 @@ __global__ void __launch_bounds__(LGB_CHUNK / R) k_eval(EvalParams P)
     }
     int c = lo;
     int q = chunk - P.chunk_start[c];
-    int pb = P.pstart[c] + q * LGB_CHUNK;
+    int nch = P.chunk_start[c + 1] - P.chunk_start[c];
+    int ncell = P.pstart[c + 1] - P.pstart[c];
+    /* the cell's particles are split evenly over its work units (no nearly empty last unit) */
+    int b0 = (int)(((long long)ncell * q) / nch), b1 = (int)(((long long)ncell * (q + 1)) / nch);
     s_cell = c;
-    s_pbeg = pb;
-    s_pn = min(LGB_CHUNK, P.pstart[c + 1] - pb);
+    s_pbeg = P.pstart[c] + b0;
+    s_pn = b1 - b0;
     s_wsum = 0;
     s_o = 0;
     s_pp = 0;
@@ -326,7 +349,7 @@ __global__ void __launch_bounds__(LGB_CHUNK / R) k_eval(EvalParams P)
   Real px[R][3];
 #pragma unroll
   for (int r = 0; r < R; r++) {
-    int idx = tid + r * EVAL_T;
+    int idx = tid * R + r; /* consecutive particles per thread: active threads fill whole warps */
     pid[r] = (idx < pn) ? P.plist[s_pbeg + idx] : -1;
     int cc[3] = {ci, cj, cl};
     for (int d = 0; d < 3; d++) {
@@ -344,6 +367,15 @@ __global__ void __launch_bounds__(LGB_CHUNK / R) k_eval(EvalParams P)
 #pragma unroll
       for (int f = 0; f < FP; f++) acc[r][k][f] = Real(0);
 
+  /* FP32: per-thread running sums of the per-patch partial sums, after the staging budget */
+  float *run = reinterpret_cast<float *>(sm + P.budget);
+  const int rstride = EVAL_T * R;
+  if constexpr (sizeof(Real) == 4) {
+#pragma unroll
+    for (int q = 0; q < NEN * FP; q++)
+#pragma unroll
+      for (int r = 0; r < R; r++) run[(size_t)q * rstride + r * EVAL_T + tid] = 0.f;
+  }
   const Real eps = (Real)g.eps_r;
   const Real ga = (Real)(-(g.eps_r * g.eps_r) * 1.4426950408889634);
   const int kernel = g.kernel;
@@ -414,7 +446,8 @@ __global__ void __launch_bounds__(LGB_CHUNK / R) k_eval(EvalParams P)
     }
     __syncthreads();
     for (int sgi = 0; sgi < nseg; sgi++)
-      eval_dispatch<Real, DIM, FP, R, KER>(s_seg_o[sgi], sm + s_seg_base[sgi], s_seg_n[sgi], px, acc, eps, ga, kernel);
+      eval_dispatch<Real, DIM, FP, R, KER>(s_seg_o[sgi], sm + s_seg_base[sgi], s_seg_n[sgi], px, acc, eps, ga, kernel,
+                                            run + tid, rstride);
     __syncthreads();
   }
 
@@ -438,8 +471,9 @@ __global__ void __launch_bounds__(LGB_CHUNK / R) k_eval(EvalParams P)
         float hi = 0.f, lo = 0.f;
 #pragma unroll
         for (int k = 0; k < NEN; k++) {
-          float prod = pw[k] * acc[r][k][f];
-          float perr = fmaf(pw[k], acc[r][k][f], -prod);
+          const float Ik = run[(size_t)(k * FP + f) * rstride + r * EVAL_T + tid];
+          float prod = pw[k] * Ik;
+          float perr = fmaf(pw[k], Ik, -prod);
           lgb_df_add(hi, lo, prod);
           lo += perr;
         }

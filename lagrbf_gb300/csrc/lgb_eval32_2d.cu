@@ -7,7 +7,8 @@ template <int DIM, int FP, int KER>
 static int launch32(const EvalParams &P, int grid, cudaStream_t s)
 {
   static bool attr = false;
-  size_t smem = (size_t)P.budget * sizeof(float);
+  /* staging budget + per-thread running sums of the NEN*FP per-patch partial sums */
+  size_t smem = ((size_t)P.budget + (size_t)(1 << DIM) * FP * LGB_CHUNK) * sizeof(float);
   if (!attr) {
     cudaFuncSetAttribute(k_eval<float, DIM, FP, 2, KER>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     attr = true;

@@ -7,8 +7,9 @@
 extern "C" int lgb_eval32_launch_3d(const EvalParams *P, int fp, int ker, int grid, void *stream);
 extern "C" int lgb_eval32_launch_2d(const EvalParams *P, int fp, int ker, int grid, void *stream);
 
-/* Staging budgets (elements): 48 KB of shared memory per CTA in both precisions. */
-#define BUDGET32 12288
+/* Staging budgets (elements): FP32 30 KB (+ up to 32 KB of running sums, four CTAs per SM),
+   FP64 48 KB. */
+#define BUDGET32 7680
 #define BUDGET64 6144
 
 template <int DIM, int FP>
