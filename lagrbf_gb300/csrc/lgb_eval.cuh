@@ -204,13 +204,14 @@ __device__ __forceinline__ void eval_dispatch(int o, const Real *rec, int n, con
 }
 
 /* Node-index range [lo, hi] along one axis that contains every node within the weight support of
-   coordinate x (conservative by one node on each side; phiW is exactly zero outside the support,
-   so extra candidates change nothing). */
+   coordinate x. */
 __device__ __forceinline__ void eval_node_range(double x, double O, double h, int n, double rad, int &lo, int &hi)
 {
+  /* nodes i with |x - (O + i h)| < rad; the 1e-6 margin (in node spacings) covers rounding, and a
+     node at distance >= rad has phiW == 0 exactly, so the range is never too small */
   const double ih = 1.0 / h;
-  int a = (int)floor((x - rad - O) * ih) - 1;
-  int b = (int)ceil((x + rad - O) * ih) + 1;
+  int a = (int)ceil((x - rad - O) * ih - 1e-6);
+  int b = (int)floor((x + rad - O) * ih + 1e-6);
   lo = (a < 0) ? 0 : a;
   hi = (b > n - 1) ? n - 1 : b;
 }
@@ -359,6 +360,8 @@ __global__ void __launch_bounds__(LGB_CHUNK / R) k_eval(EvalParams P)
       else px[r][d] = xv;
     }
   }
+  /* warps without particles stage records and meet the barriers but skip the arithmetic */
+  const bool warp_active = __any_sync(0xffffffffu, pid[0] >= 0);
   Real acc[R][NEN][FP];
 #pragma unroll
   for (int r = 0; r < R; r++)
@@ -445,9 +448,10 @@ __global__ void __launch_bounds__(LGB_CHUNK / R) k_eval(EvalParams P)
       }
     }
     __syncthreads();
-    for (int sgi = 0; sgi < nseg; sgi++)
-      eval_dispatch<Real, DIM, FP, R, KER>(s_seg_o[sgi], sm + s_seg_base[sgi], s_seg_n[sgi], px, acc, eps, ga, kernel,
-                                            run + tid, rstride);
+    if (warp_active)
+      for (int sgi = 0; sgi < nseg; sgi++)
+        eval_dispatch<Real, DIM, FP, R, KER>(s_seg_o[sgi], sm + s_seg_base[sgi], s_seg_n[sgi], px, acc, eps, ga,
+                                              kernel, run + tid, rstride);
     __syncthreads();
   }
 
