@@ -48,6 +48,7 @@ def parse():
     ap.add_argument("--cpu-sample", type=int, default=256, help="particles per emulated rank")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--profile-only", action="store_true", help="setup + a few steps, for ncu")
+    ap.add_argument("--quick", action="store_true", help="only the FP32 timed loop and the roofline pass")
     return ap.parse_args()
 
 
@@ -257,6 +258,11 @@ def main():
                 "hbm_achieved_gbs": eval_gbs, "hbm_peak_gbs": pk.get("hbm_gbs"),
                 "hbm_frac": eval_gbs / pk["hbm_gbs"] if pk.get("hbm_gbs") else None, "hbm_peak_kind": pk_kind,
                 "eval_share_of_step": (sp["eval_ms"] / nprof) / (1e3 * el / args.steps)}
+    if args.quick:
+        print(json.dumps({"quick": True, "value": value, "ms_per_step": 1e3 * el_max / args.steps,
+                          "eval_ms_per_launch": roofline["per_launch_ms"], "frac": roofline["frac"],
+                          "chunk_cap": st["chunk_cap"], "records": st["records"], "np": npart}))
+        return 0
     # ---------------- FP32 vs FP64 error after one step from the same state ----------------
     def snapshot():
         x = np.zeros((npart, 3)); f = np.zeros((npart, 3)); p = np.zeros(npart, dtype=np.int64)
@@ -329,7 +335,8 @@ def main():
                        "l2": "inputs larger than L2 (particle state %.1f GB)" % (npart * 8 * 3 * 12 / 1e9),
                        "parallelism": "replicas x%d (particles sharded, data replicated)" % world,
                        "setup_s": setup_s, "patches_factored": st0["patches_factored"],
-                       "max_patch": st0["max_patch"]},
+                       "max_patch": st0["max_patch"], "work_unit": st["chunk_cap"],
+                       "staging": "TMA bulk copies of precomputed record blocks" if st["records"] else "gather"},
             "fp64": {"value": value64, "unit": "particle-steps/s", "steps": args.fp64_steps,
                      "fp32_speedup": value / value64 if value64 > 0 else None,
                      "fp32_vs_fp64_max_rel_err": err_max, "fp32_vs_fp64_rms_rel_err": err_rms,

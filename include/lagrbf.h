@@ -117,6 +117,8 @@ typedef struct {
   int32_t max_patch;          /* largest patch (data points)                                 */
   int32_t npatch_setup;       /* patches currently set up                                    */
   double  dt;                 /* the advection context's current time step                   */
+  int32_t chunk_cap;          /* particles per evaluation work unit                          */
+  int32_t records;            /* 1 when precomputed record blocks are streamed by TMA         */
 } lagrbf_stats_t;
 
 /* The interpolated advection loop of lagrbf_advect_interpolate over [time, time_next] without its

@@ -45,6 +45,7 @@ class Stats(ctypes.Structure):
         ("steps", ctypes.c_int64), ("patches_factored", ctypes.c_int64), ("factor_ms", ctypes.c_double),
         ("factor_flops", ctypes.c_double), ("np_alive", ctypes.c_int32), ("nd", ctypes.c_int32),
         ("max_patch", ctypes.c_int32), ("npatch_setup", ctypes.c_int32), ("dt", ctypes.c_double),
+        ("chunk_cap", ctypes.c_int32), ("records", ctypes.c_int32),
     ]
 
     def as_dict(self):

@@ -329,11 +329,11 @@ extern "C" int lgb_op_data_values(lgb_dev *d, void *stream)
 /* ------------------------------------------------------------------------------------------- */
 /* particle binning per stage                                                                   */
 /* ------------------------------------------------------------------------------------------- */
-__global__ void k_chunks(int ncells, const int *__restrict__ pstart, int *__restrict__ nch)
+__global__ void k_chunks(int ncells, int cap, const int *__restrict__ pstart, int *__restrict__ nch)
 {
   int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= ncells) return;
-  nch[c] = lgb_cdiv(pstart[c + 1] - pstart[c], LGB_CHUNK);
+  nch[c] = lgb_cdiv(pstart[c + 1] - pstart[c], cap);
 }
 
 extern "C" int lgb_op_bin_particles(lgb_dev *d, int mark_dead, void *stream)
@@ -347,7 +347,7 @@ extern "C" int lgb_op_bin_particles(lgb_dev *d, int mark_dead, void *stream)
     return rc;
   if ((rc = lgb_op_scan_i32(g.ncells, d->pcount, d->pstart, d->scan_tmp, stream))) return rc;
   if ((rc = lgb_op_scatter(d->np, d->cell_p, d->alive, d->pstart, d->pfill, d->plist, stream))) return rc;
-  k_chunks<<<lgb_cdiv(g.ncells, 256), 256, 0, s>>>(g.ncells, d->pstart, d->pfill);
+  k_chunks<<<lgb_cdiv(g.ncells, 256), 256, 0, s>>>(g.ncells, d->chunk_cap, d->pstart, d->pfill);
   lgb_count_launch(1);
   LGB_CHECK_LAUNCH();
   return lgb_op_scan_i32(g.ncells, d->pfill, d->chunk_start, d->scan_tmp, stream);

@@ -9,7 +9,7 @@
  *   w_k(x)   = phiW(|x - c_k|, eps_w) / sum_{all nodes n} phiW(|x - c_n|, eps_w)     (Wendland C2)
  *
  * GB300 design.  Particles are binned by cell every stage; one CTA evaluates one work unit of up to
- * LGB_CHUNK particles of one cell.  The CTA walks the 3^dim neighbour cells of its cell in the
+ * chunk_cap particles of one cell.  The CTA walks the 3^dim neighbour cells of its cell in the
  * reference's neighbour order, staging for each neighbour cell a record per data point
  * {x, y, z, pad, X_k[j, f] for every corner patch k of the particle's cell that contains the
  * neighbour cell} in shared memory (a fixed budget, refilled in rounds when the block does not
@@ -49,7 +49,10 @@ struct EvalParams {
   double *out;
   int out_stride;
   lgb_ctrl *ctrl;
-  int budget;             /* staging budget, elements of the compute type */
+  int budget;             /* staging budget, elements of the compute type (per buffer) */
+  int chunk_cap;          /* particles per work unit (blockDim.x * R)     */
+  float *rec32;           /* precomputed FP32 record blocks (TMA staging)  */
+  const long long *rec_off;
 };
 
 enum { KER_GENERIC = 0, KER_C2 = 1, KER_GAUSS = 2 };
@@ -96,7 +99,8 @@ template <typename Real, int KER>
 __device__ __forceinline__ Real eval_phi(Real d2, Real eps, Real ga, int kernel)
 {
   if constexpr (sizeof(Real) == 4 && KER == KER_C2) {
-    float r = d2 * rsqrtf(fmaxf(d2, 1e-30f));
+    float r;
+    asm("sqrt.approx.f32 %0, %1;" : "=f"(r) : "f"(d2)); /* one MUFU op; exact at 0 */
     float u = fmaxf(1.0f - eps * r, 0.0f);
     float u2 = u * u;
     return (u2 * u2) * (5.0f - 4.0f * u);
@@ -171,7 +175,7 @@ __device__ __forceinline__ void eval_segment(const Real *__restrict__ rec, int n
         for (int f = 0; f < FP; f++)
 #pragma unroll
           for (int r = 0; r < R; r++) {
-            float *q = run + (size_t)(k * FP + f) * rstride + r * (rstride / R);
+            float *q = run + (r * NEN + k) * FP + f; /* this thread's slot block (compile-time offsets) */
             *q += acc[r][k][f];
             acc[r][k][f] = 0.f;
           }
@@ -280,16 +284,166 @@ __device__ __forceinline__ void eval_weights(const lgb_geom &g, int ci, int cj, 
   }
 }
 
-template <typename Real, int DIM, int FP, int R, int KER>
-__global__ void __launch_bounds__(LGB_CHUNK / R) k_eval(EvalParams P)
+/* One record of the staged block: coordinates of data point `sidx` (neighbour offset o, position
+   pp inside its cell) relative to the origin of cell (ci, cj, cl), then the FP coefficients of every
+   corner patch k of that cell containing the neighbour cell (zeros for patches not set up),
+   zero-padded to the record length. */
+template <typename Real, int DIM, int FP>
+__device__ __forceinline__ void write_record(const EvalParams &P, int o, int pp, int sidx, const int *node,
+                                             const int *setup, Real *rec)
+{
+  constexpr int NEN = EGeo<DIM>::NEN;
+  const int mask = einv_mask(DIM, o);
+  const int S = erec<Real>(epopc(mask), FP);
+  if constexpr (sizeof(Real) == 4) {
+    const float4 xr = reinterpret_cast<const float4 *>(P.xr32)[sidx];
+    rec[0] = xr.x + eoff_a(o) * (float)P.g.h[0];
+    rec[1] = xr.y + eoff_b(o) * (float)P.g.h[1];
+    rec[2] = (DIM == 3) ? xr.z + eoff_e(DIM, o) * (float)P.g.h[2] : 0.f;
+    rec[3] = 0.f;
+  } else {
+    rec[0] = P.xs64[(size_t)sidx * DIM + 0];
+    rec[1] = P.xs64[(size_t)sidx * DIM + 1];
+    rec[2] = (DIM == 3) ? P.xs64[(size_t)sidx * DIM + 2] : 0.0;
+    rec[3] = 0.0;
+  }
+  int j = 0;
+  for (int k = 0; k < NEN; k++) {
+    if (!((mask >> k) & 1)) continue;
+    Real *dst = rec + 4 + j * FP;
+    if (setup[k]) {
+      const long long pos = P.coff[node[k]] + P.slot[node[k] * 8 + eslot(DIM, k, o)] + pp;
+      const size_t src = (size_t)pos * P.F + P.f0;
+      for (int f = 0; f < FP; f++) {
+        if constexpr (sizeof(Real) == 4) dst[f] = P.c32[src + f];
+        else dst[f] = P.c64[src + f];
+      }
+    } else {
+      for (int f = 0; f < FP; f++) dst[f] = Real(0);
+    }
+    j++;
+  }
+  for (int q = 4 + j * FP; q < S; q++) rec[q] = Real(0);
+}
+
+/* Per-CTA description of a cell's evaluation block: neighbour counts, first sorted index, corner
+   nodes and their set-up state. */
+template <int DIM>
+__device__ __forceinline__ void cell_block(const EvalParams &P, int cell, int *s_cnt, int *s_first, int *s_node,
+                                           int *s_setup)
 {
   constexpr int NEN = EGeo<DIM>::NEN, NOFF = EGeo<DIM>::NOFF;
-  constexpr int EVAL_T = LGB_CHUNK / R;
+  const lgb_geom &g = P.g;
+  const int tid = threadIdx.x;
+  int ci, cj, cl;
+  lgb_cell_ijk(g, cell, ci, cj, cl);
+  if (tid < NOFF) {
+    int ni = ci + eoff_a(tid), nj = cj + eoff_b(tid), nl = cl + eoff_e(DIM, tid);
+    int cnt = 0, first = 0;
+    if (ni >= 0 && ni < g.nc[0] && nj >= 0 && nj < g.nc[1] && nl >= 0 && nl < g.nc[2]) {
+      int nb = ni + nj * g.nc[0] + nl * g.nc[0] * g.nc[1];
+      first = P.cstart[nb];
+      cnt = P.cstart[nb + 1] - first;
+    }
+    s_cnt[tid] = cnt;
+    s_first[tid] = first;
+  }
+  if (tid < NEN) {
+    int node = (ci + ecorner_ox(tid)) + (cj + ecorner_oy(tid)) * g.n[0] + (cl + ecorner_oz(DIM, tid)) * g.n[0] * g.n[1];
+    s_node[tid] = node;
+    s_setup[tid] = P.setup[node];
+  }
+}
+
+/* Builds the staged record blocks of every cell into P.rec32 (FP32, FP fields from field f0), in
+   neighbour-offset order, at P.rec_off[cell].  Runs only when `force` or when the preceding
+   factorisation launch set up or solved at least one patch (device-side count), so the launch can
+   sit in the captured step graph. */
+template <int DIM, int FP>
+__global__ void __launch_bounds__(128) k_build_records(EvalParams P, int force)
+{
+  constexpr int NOFF = EGeo<DIM>::NOFF;
+  __shared__ int s_cnt[27], s_first[27], s_node[8], s_setup[8];
+  if (!force && P.ctrl->nwork == 0) return;
+  for (int cell = blockIdx.x; cell < P.g.ncells; cell += gridDim.x) {
+    cell_block<DIM>(P, cell, s_cnt, s_first, s_node, s_setup);
+    __syncthreads();
+    float *dst = P.rec32 + P.rec_off[cell];
+    for (int o = 0; o < NOFF; o++) {
+      const int S = erec<float>(epopc(einv_mask(DIM, o)), FP);
+      for (int p = threadIdx.x; p < s_cnt[o]; p += blockDim.x)
+        write_record<float, DIM, FP>(P, o, p, s_first[o] + p, s_node, s_setup, dst + (size_t)p * S);
+      dst += (size_t)s_cnt[o] * S;
+    }
+    __syncthreads();
+  }
+}
+
+/* ---- TMA bulk copies into shared memory, completion tracked by an mbarrier ---- */
+__device__ __forceinline__ unsigned smem_addr(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void tma_issue(float *dst, const float *src, unsigned bytes, unsigned long long *mbar)
+{
+  const unsigned mb = smem_addr(mbar), d = smem_addr(dst);
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mb), "r"(bytes) : "memory");
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+               ::"r"(d), "l"(src), "r"(bytes), "r"(mb) : "memory");
+}
+
+/* Bounded wait for the phase `parity` of an mbarrier; false if it did not complete. */
+__device__ __forceinline__ bool tma_wait(unsigned long long *mbar, unsigned parity)
+{
+  const unsigned mb = smem_addr(mbar);
+  for (int it = 0; it < (1 << 22); ++it) {
+    unsigned done;
+    asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+                 : "=r"(done) : "r"(mb), "r"(parity) : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+
+/* Round planner (one thread): packs the next records of the block, in neighbour order, into a
+   staging buffer of `budget` elements; advances the cursor (o, pp) and returns the elements planned. */
+template <typename Real, int DIM, int FP>
+__device__ __noinline__ int eval_plan(const int *cnt, int budget, int &o, int &pp, int *seg_o, int *seg_p0, int *seg_n,
+                                      int *seg_base, int *nseg_out)
+{
+  constexpr int NOFF = EGeo<DIM>::NOFF;
+  int base = 0, nseg = 0;
+  while (o < NOFF) {
+    int c = cnt[o] - pp;
+    if (c <= 0) { o++; pp = 0; continue; }
+    int S = erec<Real>(epopc(einv_mask(DIM, o)), FP);
+    int fit = (budget - base) / S;
+    if (fit <= 0) break;
+    int take = min(c, fit);
+    seg_o[nseg] = o; seg_p0[nseg] = pp; seg_n[nseg] = take; seg_base[nseg] = base;
+    nseg++;
+    base += take * S;
+    pp += take;
+    if (pp >= cnt[o]) { o++; pp = 0; }
+  }
+  *nseg_out = nseg;
+  return base;
+}
+
+/* STAGE: 0 = gather the records from the coefficient pool each round (any precision, any field
+   range); 1 = stream precomputed FP32 record blocks with TMA bulk copies into two shared-memory
+   buffers (the next round's copy is in flight while the current round computes). */
+template <typename Real, int DIM, int FP, int R, int KER, int STAGE>
+__global__ void __launch_bounds__(LGB_CHUNK_MAX / R) k_eval(EvalParams P)
+{
+  constexpr int NEN = EGeo<DIM>::NEN, NOFF = EGeo<DIM>::NOFF;
+  const int EVAL_T = blockDim.x; /* work-unit capacity = EVAL_T * R particles (P.chunk_cap) */
   extern __shared__ __align__(16) unsigned char smem_raw[];
   Real *sm = reinterpret_cast<Real *>(smem_raw);
   __shared__ int s_cnt[27], s_first[27], s_node[8], s_setup[8];
-  __shared__ int s_seg_o[27], s_seg_p0[27], s_seg_n[27], s_seg_base[27];
-  __shared__ int s_nseg, s_o, s_pp, s_cell, s_pbeg, s_pn, s_blk, s_wsum;
+  __shared__ int s_seg_o[2][27], s_seg_p0[2][27], s_seg_n[2][27], s_seg_base[2][27], s_nseg[2];
+  __shared__ long long s_pre[28];
+  __shared__ __align__(8) unsigned long long s_mbar[2];
+  __shared__ int s_o, s_pp, s_cell, s_pbeg, s_pn, s_blk, s_wsum;
   const lgb_geom &g = P.g;
   const int tid = threadIdx.x;
   const int chunk = blockIdx.x;
@@ -318,28 +472,18 @@ __global__ void __launch_bounds__(LGB_CHUNK / R) k_eval(EvalParams P)
   const int cell = s_cell;
   int ci, cj, cl;
   lgb_cell_ijk(g, cell, ci, cj, cl);
-  if (tid < NOFF) {
-    int a = eoff_a(tid), b = eoff_b(tid), e = eoff_e(DIM, tid);
-    int ni = ci + a, nj = cj + b, nl = cl + e;
-    int cnt = 0, first = 0;
-    if (ni >= 0 && ni < g.nc[0] && nj >= 0 && nj < g.nc[1] && nl >= 0 && nl < g.nc[2]) {
-      int nb = ni + nj * g.nc[0] + nl * g.nc[0] * g.nc[1];
-      first = P.cstart[nb];
-      cnt = P.cstart[nb + 1] - first;
-    }
-    s_cnt[tid] = cnt;
-    s_first[tid] = first;
-  }
-  if (tid < NEN) {
-    int node = (ci + ecorner_ox(tid)) + (cj + ecorner_oy(tid)) * g.n[0] + (cl + ecorner_oz(DIM, tid)) * g.n[0] * g.n[1];
-    s_node[tid] = node;
-    s_setup[tid] = P.setup[node];
-  }
+  cell_block<DIM>(P, cell, s_cnt, s_first, s_node, s_setup);
   __syncthreads();
   if (tid == 0) {
-    int b = 0;
-    for (int o = 0; o < NOFF; o++) b += s_cnt[o];
-    s_blk = b;
+    long long b = 0;
+    for (int o = 0; o < NOFF; o++) {
+      s_pre[o] = b;
+      b += (long long)s_cnt[o] * erec<Real>(epopc(einv_mask(DIM, o)), FP);
+    }
+    s_pre[NOFF] = b;
+    int nb = 0;
+    for (int o = 0; o < NOFF; o++) nb += s_cnt[o];
+    s_blk = nb;
   }
   __syncthreads();
   if (s_blk == 0) return; /* empty neighbourhood: the value is left untouched (interpolation.c:89) */
@@ -370,89 +514,85 @@ __global__ void __launch_bounds__(LGB_CHUNK / R) k_eval(EvalParams P)
 #pragma unroll
       for (int f = 0; f < FP; f++) acc[r][k][f] = Real(0);
 
-  /* FP32: per-thread running sums of the per-patch partial sums, after the staging budget */
-  float *run = reinterpret_cast<float *>(sm + P.budget);
-  const int rstride = EVAL_T * R;
+  /* shared memory: [staging buffer 0 | staging buffer 1 (TMA only)] [FP32 running sums: one block of
+     R*NEN*FP (+1 pad, odd stride: no bank conflicts) floats per thread] */
+  const int nbuf = (STAGE == 1) ? 2 : 1;
+  constexpr int RUNB = R * NEN * FP + 1;
+  float *run = reinterpret_cast<float *>(sm + (size_t)nbuf * P.budget) + (size_t)tid * RUNB;
+  const int rstride = 0;
   if constexpr (sizeof(Real) == 4) {
 #pragma unroll
-    for (int q = 0; q < NEN * FP; q++)
-#pragma unroll
-      for (int r = 0; r < R; r++) run[(size_t)q * rstride + r * EVAL_T + tid] = 0.f;
+    for (int q = 0; q < R * NEN * FP; q++) run[q] = 0.f;
   }
   const Real eps = (Real)g.eps_r;
   const Real ga = (Real)(-(g.eps_r * g.eps_r) * 1.4426950408889634);
   const int kernel = g.kernel;
-  const Real hh[3] = {(Real)g.h[0], (Real)g.h[1], (Real)g.h[2]};
 
-  for (;;) {
+  if constexpr (STAGE == 1) {
     if (tid == 0) {
-      int o = s_o, pp = s_pp, base = 0, nseg = 0;
-      while (o < NOFF) {
-        int cnt = s_cnt[o] - pp;
-        if (cnt <= 0) { o++; pp = 0; continue; }
-        int S = erec<Real>(epopc(einv_mask(DIM, o)), FP);
-        int fit = (P.budget - base) / S;
-        if (fit <= 0) break;
-        int take = min(cnt, fit);
-        s_seg_o[nseg] = o; s_seg_p0[nseg] = pp; s_seg_n[nseg] = take; s_seg_base[nseg] = base;
-        nseg++;
-        base += take * S;
-        pp += take;
-        if (pp >= s_cnt[o]) { o++; pp = 0; }
-      }
-      s_nseg = nseg; s_o = o; s_pp = pp;
-    }
-    __syncthreads();
-    const int nseg = s_nseg;
-    if (nseg == 0) break;
-    /* fill the staged records */
-    for (int sgi = 0; sgi < nseg; sgi++) {
-      const int o = s_seg_o[sgi], p0 = s_seg_p0[sgi], n = s_seg_n[sgi];
-      const int mask = einv_mask(DIM, o);
-      const int S = erec<Real>(epopc(mask), FP);
-      Real *rbase = sm + s_seg_base[sgi];
-      const int a = eoff_a(o), b = eoff_b(o), e = eoff_e(DIM, o);
-      for (int p = tid; p < n; p += EVAL_T) {
-        const int s = s_first[o] + p0 + p;
-        Real *rec = rbase + (size_t)p * S;
-        if constexpr (sizeof(Real) == 4) {
-          float4 xr = reinterpret_cast<const float4 *>(P.xr32)[s];
-          rec[0] = xr.x + a * hh[0];
-          rec[1] = xr.y + b * hh[1];
-          rec[2] = (DIM == 3) ? xr.z + e * hh[2] : 0.f;
-          rec[3] = 0.f;
-        } else {
-          rec[0] = P.xs64[(size_t)s * DIM + 0];
-          rec[1] = P.xs64[(size_t)s * DIM + 1];
-          rec[2] = (DIM == 3) ? P.xs64[(size_t)s * DIM + 2] : 0.0;
-          rec[3] = 0.0;
-        }
-        int j = 0;
-        for (int k = 0; k < NEN; k++) {
-          if (!((mask >> k) & 1)) continue;
-          const int node = s_node[k];
-          Real *dst = rec + 4 + j * FP;
-          if (s_setup[k]) {
-            long long pos = P.coff[node] + P.slot[node * 8 + eslot(DIM, k, o)] + p0 + p;
-            const size_t src = (size_t)pos * P.F + P.f0;
-            for (int f = 0; f < FP; f++) {
-              if constexpr (sizeof(Real) == 4) dst[f] = P.c32[src + f];
-              else dst[f] = P.c64[src + f];
-            }
-          } else {
-            for (int f = 0; f < FP; f++) dst[f] = Real(0);
-          }
-          j++;
-        }
-        for (int q = 4 + j * FP; q < S; q++) rec[q] = Real(0);
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&s_mbar[0])) : "memory");
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&s_mbar[1])) : "memory");
+      asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+      const int o0 = s_o, pp0 = s_pp;
+      int o = s_o, pp = s_pp;
+      const int n = eval_plan<Real, DIM, FP>(s_cnt, P.budget, o, pp, s_seg_o[0], s_seg_p0[0], s_seg_n[0], s_seg_base[0],
+                                             &s_nseg[0]);
+      s_o = o; s_pp = pp;
+      if (n > 0) {
+        const float *src = P.rec32 + P.rec_off[cell] + s_pre[o0] + (long long)pp0 * erec<float>(epopc(einv_mask(DIM, o0)), FP);
+        tma_issue(reinterpret_cast<float *>(sm), src, (unsigned)n * 4u, &s_mbar[0]);
       }
     }
     __syncthreads();
-    if (warp_active)
-      for (int sgi = 0; sgi < nseg; sgi++)
-        eval_dispatch<Real, DIM, FP, R, KER>(s_seg_o[sgi], sm + s_seg_base[sgi], s_seg_n[sgi], px, acc, eps, ga,
-                                              kernel, run + tid, rstride);
-    __syncthreads();
+    for (int r = 0;; r++) {
+      const int b = r & 1;
+      const int nseg = s_nseg[b];
+      if (nseg == 0) break;
+      if (tid == 0) {
+        const int o0 = s_o, pp0 = s_pp;
+        int o = s_o, pp = s_pp;
+        const int n = eval_plan<Real, DIM, FP>(s_cnt, P.budget, o, pp, s_seg_o[b ^ 1], s_seg_p0[b ^ 1], s_seg_n[b ^ 1],
+                                               s_seg_base[b ^ 1], &s_nseg[b ^ 1]);
+        s_o = o; s_pp = pp;
+        if (n > 0) {
+          const float *src = P.rec32 + P.rec_off[cell] + s_pre[o0] + (long long)pp0 * erec<float>(epopc(einv_mask(DIM, o0)), FP);
+          tma_issue(reinterpret_cast<float *>(sm) + (size_t)(b ^ 1) * P.budget, src, (unsigned)n * 4u, &s_mbar[b ^ 1]);
+        }
+      }
+      const bool ok = tma_wait(&s_mbar[b], (unsigned)((r >> 1) & 1));
+      if (!ok && tid == 0) atomicExch(&P.ctrl->eval_error, 1);
+      if (ok && warp_active) {
+        const Real *buf = sm + (size_t)b * P.budget;
+        for (int sgi = 0; sgi < nseg; sgi++)
+          eval_dispatch<Real, DIM, FP, R, KER>(s_seg_o[b][sgi], buf + s_seg_base[b][sgi], s_seg_n[b][sgi], px, acc,
+                                                eps, ga, kernel, run, rstride);
+      }
+      __syncthreads();
+    }
+  } else {
+    for (;;) {
+      if (tid == 0) {
+        int o = s_o, pp = s_pp;
+        eval_plan<Real, DIM, FP>(s_cnt, P.budget, o, pp, s_seg_o[0], s_seg_p0[0], s_seg_n[0], s_seg_base[0], &s_nseg[0]);
+        s_o = o; s_pp = pp;
+      }
+      __syncthreads();
+      const int nseg = s_nseg[0];
+      if (nseg == 0) break;
+      for (int sgi = 0; sgi < nseg; sgi++) {
+        const int o = s_seg_o[0][sgi], p0 = s_seg_p0[0][sgi], n = s_seg_n[0][sgi];
+        const int S = erec<Real>(epopc(einv_mask(DIM, o)), FP);
+        Real *rbase = sm + s_seg_base[0][sgi];
+        for (int p = tid; p < n; p += EVAL_T)
+          write_record<Real, DIM, FP>(P, o, p0 + p, s_first[o] + p0 + p, s_node, s_setup, rbase + (size_t)p * S);
+      }
+      __syncthreads();
+      if (warp_active)
+        for (int sgi = 0; sgi < nseg; sgi++)
+          eval_dispatch<Real, DIM, FP, R, KER>(s_seg_o[0][sgi], sm + s_seg_base[0][sgi], s_seg_n[0][sgi], px, acc,
+                                                eps, ga, kernel, run, rstride);
+      __syncthreads();
+    }
   }
 
   /* epilogue: PU weights and the weighted sum */
@@ -475,7 +615,7 @@ __global__ void __launch_bounds__(LGB_CHUNK / R) k_eval(EvalParams P)
         float hi = 0.f, lo = 0.f;
 #pragma unroll
         for (int k = 0; k < NEN; k++) {
-          const float Ik = run[(size_t)(k * FP + f) * rstride + r * EVAL_T + tid];
+          const float Ik = run[(r * NEN + k) * FP + f];
           float prod = pw[k] * Ik;
           float perr = fmaf(pw[k], Ik, -prod);
           lgb_df_add(hi, lo, prod);
@@ -497,8 +637,8 @@ __global__ void __launch_bounds__(LGB_CHUNK / R) k_eval(EvalParams P)
       for (int f = 0; f < FP; f++) o[f] = val[f];
     }
   }
-  /* algorithmic work of this unit (SURVEY-style count: distances 10, kernel k_phi, 2 flops per
-     coefficient FMA, 18 per support node of the weights, 2F+1 per corner in the epilogue) */
+  /* algorithmic work of this unit: distances 10 flops, kernel k_phi, 2 flops per coefficient FMA,
+     18 per support node of the weights, 2F+1 per corner in the epilogue */
   for (int off = 16; off > 0; off >>= 1) wloc += __shfl_down_sync(0xffffffffu, wloc, off);
   if ((tid & 31) == 0) atomicAdd(&s_wsum, wloc);
   __syncthreads();

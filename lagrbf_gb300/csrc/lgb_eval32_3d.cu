@@ -1,37 +1,46 @@
 /*
- * lgb_eval32_3d.cu -- FP32-evaluation instantiations (3D) of the PU evaluation kernel (lgb_eval.cuh).
+ * lgb_eval32_3d.cu -- FP32-evaluation instantiations of the PU evaluation kernel (lgb_eval.cuh), 3D.
  */
 #include "lgb_eval.cuh"
 
-template <int DIM, int FP, int KER>
+template <int DIM, int FP, int KER, int STAGE>
 static int launch32(const EvalParams &P, int grid, cudaStream_t s)
 {
   static bool attr = false;
-  /* staging budget + per-thread running sums of the NEN*FP per-patch partial sums */
-  size_t smem = ((size_t)P.budget + (size_t)(1 << DIM) * FP * LGB_CHUNK) * sizeof(float);
+  const int nbuf = (STAGE == 1) ? 2 : 1;
+  /* staging buffer(s) + per-thread running sums of the NEN*FP per-patch partial sums */
+  size_t smem = ((size_t)nbuf * P.budget + (size_t)(2 * (1 << DIM) * FP + 1) * (P.chunk_cap / 2)) * sizeof(float);
   if (!attr) {
-    cudaFuncSetAttribute(k_eval<float, DIM, FP, 2, KER>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    size_t smax = ((size_t)nbuf * P.budget + (size_t)(2 * (1 << DIM) * FP + 1) * (LGB_CHUNK_MAX / 2)) * sizeof(float);
+    cudaFuncSetAttribute(k_eval<float, DIM, FP, 2, KER, STAGE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smax);
     attr = true;
   }
-  k_eval<float, DIM, FP, 2, KER><<<grid, LGB_CHUNK / 2, smem, s>>>(P);
+  k_eval<float, DIM, FP, 2, KER, STAGE><<<grid, P.chunk_cap / 2, smem, s>>>(P);
   return (int)cudaGetLastError();
 }
 
 template <int DIM, int KER>
-static int launch32_fp(const EvalParams &P, int fp, int grid, cudaStream_t s)
+static int launch32_fp(const EvalParams &P, int fp, int stage, int grid, cudaStream_t s)
 {
+  if (stage == 1) return launch32<DIM, DIM, KER, 1>(P, grid, s); /* records hold the dim velocity fields */
   switch (fp) {
-  case 1: return launch32<DIM, 1, KER>(P, grid, s);
-  case 2: return launch32<DIM, 2, KER>(P, grid, s);
-  case 3: return launch32<DIM, 3, KER>(P, grid, s);
-  default: return launch32<DIM, 4, KER>(P, grid, s);
+  case 1: return launch32<DIM, 1, KER, 0>(P, grid, s);
+  case 2: return launch32<DIM, 2, KER, 0>(P, grid, s);
+  case 3: return launch32<DIM, 3, KER, 0>(P, grid, s);
+  default: return launch32<DIM, 4, KER, 0>(P, grid, s);
   }
 }
 
-extern "C" int lgb_eval32_launch_3d(const EvalParams *P, int fp, int ker, int grid, void *stream)
+extern "C" int lgb_eval32_launch_3d(const EvalParams *P, int fp, int ker, int stage, int grid, void *stream)
 {
   cudaStream_t s = (cudaStream_t)stream;
-  if (ker == KER_C2) return launch32_fp<3, KER_C2>(*P, fp, grid, s);
-  if (ker == KER_GAUSS) return launch32_fp<3, KER_GAUSS>(*P, fp, grid, s);
-  return launch32_fp<3, KER_GENERIC>(*P, fp, grid, s);
+  if (ker == KER_C2) return launch32_fp<3, KER_C2>(*P, fp, stage, grid, s);
+  if (ker == KER_GAUSS) return launch32_fp<3, KER_GAUSS>(*P, fp, stage, grid, s);
+  return launch32_fp<3, KER_GENERIC>(*P, fp, stage, grid, s);
+}
+
+extern "C" int lgb_build_records_3d(const EvalParams *P, int force, int grid, void *stream)
+{
+  k_build_records<3, 3><<<grid, 128, 0, (cudaStream_t)stream>>>(*P, force);
+  return (int)cudaGetLastError();
 }

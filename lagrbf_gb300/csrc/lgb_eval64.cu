@@ -3,13 +3,17 @@
  * lgb_op_eval and the FP64 PU-weights kernel.
  */
 #include "lgb_eval.cuh"
+#include <string.h>
 
-extern "C" int lgb_eval32_launch_3d(const EvalParams *P, int fp, int ker, int grid, void *stream);
-extern "C" int lgb_eval32_launch_2d(const EvalParams *P, int fp, int ker, int grid, void *stream);
+extern "C" int lgb_eval32_launch_3d(const EvalParams *P, int fp, int ker, int stage, int grid, void *stream);
+extern "C" int lgb_eval32_launch_2d(const EvalParams *P, int fp, int ker, int stage, int grid, void *stream);
+extern "C" int lgb_build_records_3d(const EvalParams *P, int force, int grid, void *stream);
+extern "C" int lgb_build_records_2d(const EvalParams *P, int force, int grid, void *stream);
 
-/* Staging budgets (elements): FP32 30 KB (+ up to 32 KB of running sums, four CTAs per SM),
-   FP64 48 KB. */
+/* Staging budgets (elements): FP32 gather 30 KB, FP32 TMA 2 x 16 KB (each + up to 32 KB of running
+   sums: four CTAs per SM), FP64 48 KB. */
 #define BUDGET32 7680
+#define BUDGET32_TMA 3584
 #define BUDGET64 6144
 
 template <int DIM, int FP>
@@ -18,11 +22,11 @@ static int launch64(const EvalParams &P, int grid, cudaStream_t s)
   static bool attr = false;
   size_t smem = (size_t)P.budget * sizeof(double);
   if (!attr) {
-    cudaFuncSetAttribute(k_eval<double, DIM, FP, 1, KER_GENERIC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaFuncSetAttribute(k_eval<double, DIM, FP, 1, KER_GENERIC, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)smem);
     attr = true;
   }
-  k_eval<double, DIM, FP, 1, KER_GENERIC><<<grid, LGB_CHUNK, smem, s>>>(P);
+  k_eval<double, DIM, FP, 1, KER_GENERIC, 0><<<grid, P.chunk_cap, smem, s>>>(P);
   return (int)cudaGetLastError();
 }
 
@@ -44,7 +48,7 @@ extern "C" int lgb_op_eval(lgb_dev *d, int nf_first, int nf, double *out, int ou
   cudaStream_t s = (cudaStream_t)stream;
   if (d->np <= 0 || nf <= 0) return 0;
   const lgb_geom &g = d->g;
-  int grid = g.ncells + lgb_cdiv(d->np, LGB_CHUNK) + 1;
+  int grid = g.ncells + lgb_cdiv(d->np, d->chunk_cap) + 1;
   int ker = (g.kernel == LGB_KERNEL_WENDLAND_C2) ? KER_C2 : (g.kernel == LGB_KERNEL_GAUSSIAN) ? KER_GAUSS : KER_GENERIC;
   for (int f = nf_first; f < nf_first + nf; f += 4) {
     int fp = nf_first + nf - f;
@@ -68,10 +72,15 @@ extern "C" int lgb_op_eval(lgb_dev *d, int nf_first, int nf, double *out, int ou
     P.out = out + (f - nf_first);
     P.out_stride = out_stride;
     P.ctrl = d->ctrl;
+    P.chunk_cap = d->chunk_cap;
+    P.rec32 = d->rec32;
+    P.rec_off = d->rec_off;
     int rc;
     if (d->prec == LGB_PREC_FP32) {
-      P.budget = BUDGET32;
-      rc = (g.dim == 3) ? lgb_eval32_launch_3d(&P, fp, ker, grid, stream) : lgb_eval32_launch_2d(&P, fp, ker, grid, stream);
+      const int stage = (d->rec32 && f == 0 && fp == g.dim && d->rec_fp == g.dim) ? 1 : 0;
+      P.budget = stage ? BUDGET32_TMA : BUDGET32;
+      rc = (g.dim == 3) ? lgb_eval32_launch_3d(&P, fp, ker, stage, grid, stream)
+                        : lgb_eval32_launch_2d(&P, fp, ker, stage, grid, stream);
     } else {
       P.budget = BUDGET64;
       rc = (g.dim == 3) ? launch64_fp<3>(P, fp, grid, s) : launch64_fp<2>(P, fp, grid, s);
@@ -80,6 +89,31 @@ extern "C" int lgb_op_eval(lgb_dev *d, int nf_first, int nf, double *out, int ou
     if (rc) return rc;
   }
   return 0;
+}
+
+/* (Re)build the precomputed FP32 record blocks; without `force` the kernel only runs when the
+   preceding factorisation processed patches (device-side count). */
+extern "C" int lgb_op_build_records(lgb_dev *d, int force, void *stream)
+{
+  if (!d->rec32 || d->F < d->g.dim) return 0;
+  EvalParams P;
+  memset(&P, 0, sizeof(P));
+  P.g = d->g;
+  P.cstart = d->cstart;
+  P.xr32 = d->xr;
+  P.c32 = d->c32;
+  P.coff = d->coff;
+  P.slot = d->slot;
+  P.setup = d->setup;
+  P.F = d->F;
+  P.f0 = 0;
+  P.ctrl = d->ctrl;
+  P.rec32 = d->rec32;
+  P.rec_off = d->rec_off;
+  int grid = d->g.ncells < 8 * d->nsm ? d->g.ncells : 8 * d->nsm;
+  int rc = (d->g.dim == 3) ? lgb_build_records_3d(&P, force, grid, stream) : lgb_build_records_2d(&P, force, grid, stream);
+  lgb_count_launch(1);
+  return rc;
 }
 
 extern "C" int lgb_op_weights(lgb_dev *d, double *w, void *stream)

@@ -281,6 +281,7 @@ static void destroy_ctx(lgb_ctx *c)
   DFREE(d->need); DFREE(d->work); DFREE(d->status); DFREE(d->coff); DFREE(d->foff); DFREE(d->c64);
   DFREE(d->c32); DFREE(d->fac); DFREE(d->ws); DFREE(d->pcount); DFREE(d->pstart); DFREE(d->pfill);
   DFREE(d->chunk_start); DFREE(d->scan_tmp); DFREE(d->scan_tmp64); DFREE(d->ctrl);
+  DFREE(d->rec32); DFREE(d->rec_off);
   for (i = 0; i < 2 * NPROF; i++) if (c->ev[i]) cudaEventDestroy(c->ev[i]);
   if (c->hctrl) cudaFreeHost(c->hctrl);
   if (c->stream) cudaStreamDestroy(c->stream);
@@ -456,6 +457,7 @@ static int create_ctx(lgb_ctx **out)
   }
   for (i = 0; i < 2 * NPROF; i++) cudaEventCreate(&c->ev[i]);
   c->launch_base = lgb_launch_count();
+  d->chunk_cap = LGB_CHUNK_MAX;
   *out = c;
   return 0;
 }
@@ -551,6 +553,58 @@ static int ensure_pools(lgb_ctx *c)
   return 0;
 }
 
+/* Offsets of the precomputed FP32 record blocks (one per cell, neighbour-offset order, dim fields per
+   corner patch) and their allocation; disabled (gather staging) when F < dim or when the blocks would
+   exceed LAGRBF_RECORDS_MAX_GB (default 16 GB). */
+static int ensure_records(lgb_ctx *c)
+{
+  lgb_dev *d = &c->d;
+  const lgb_geom *g = &d->g;
+  int nc = g->ncells, cell, o, err = 0;
+  int noff = (g->dim == 3) ? 27 : 9;
+  int *cs;
+  long long *off, total = 0, maxbytes = 16LL << 30;
+  const char *env = getenv("LAGRBF_RECORDS_MAX_GB");
+  if (env) maxbytes = (long long)(atof(env) * (double)(1LL << 30));
+  d->rec_fp = g->dim;
+  if (d->F < g->dim || maxbytes <= 0) { DFREE(d->rec32); d->rec_cap = 0; return 0; }
+  cs = (int *)malloc(sizeof(int) * (size_t)(nc + 1));
+  off = (long long *)malloc(sizeof(long long) * (size_t)(nc + 1));
+  if (!cs || !off) { free(cs); free(off); return set_error(LAGRBF_ERR_MEM, "out of host memory"); }
+  CU(cudaMemcpy(cs, d->cstart, sizeof(int) * (size_t)(nc + 1), cudaMemcpyDeviceToHost));
+  for (cell = 0; cell < nc; cell++) {
+    int cxy = g->nc[0] * g->nc[1], l = cell / cxy, r = cell - l * cxy, j = r / g->nc[0], i = r - j * g->nc[0];
+    off[cell] = total;
+    for (o = 0; o < noff; o++) {
+      int a = o % 3 - 1, b = (o / 3) % 3 - 1, e = (g->dim == 3) ? o / 9 - 1 : 0;
+      int ni = i + a, nj = j + b, nl = l + e, nb, ninv, S;
+      if (ni < 0 || ni >= g->nc[0] || nj < 0 || nj >= g->nc[1] || nl < 0 || nl >= g->nc[2]) continue;
+      nb = ni + nj * g->nc[0] + nl * cxy;
+      ninv = (a == 0 ? 2 : 1) * (b == 0 ? 2 : 1) * ((g->dim == 3 && e == 0) ? 2 : 1);
+      S = ((4 + ninv * g->dim + 3) / 4) * 4;
+      total += (long long)(cs[nb + 1] - cs[nb]) * S;
+    }
+  }
+  off[nc] = total;
+  free(cs);
+  if (total * 4 > maxbytes) {
+    free(off);
+    DFREE(d->rec32);
+    d->rec_cap = 0;
+    return 0;
+  }
+  if (!d->rec_off) d->rec_off = (long long *)dalloc(sizeof(long long) * (size_t)(nc + 1), &err);
+  if (total > d->rec_cap) {
+    DFREE(d->rec32);
+    d->rec32 = (float *)dalloc(sizeof(float) * (size_t)(total > 0 ? total : 4), &err);
+    d->rec_cap = err ? 0 : total;
+  }
+  if (err) { free(off); DFREE(d->rec32); d->rec_cap = 0; return 0; /* fall back to gather staging */ }
+  CU(cudaMemcpy(d->rec_off, off, sizeof(long long) * (size_t)(nc + 1), cudaMemcpyHostToDevice));
+  free(off);
+  return 0;
+}
+
 static int fill_data(lgb_ctx *c, int n, const double *coords, const double *values, const int64_t *pidx)
 {
   lgb_dev *d = &c->d;
@@ -586,6 +640,7 @@ static int fill_data(lgb_ctx *c, int n, const double *coords, const double *valu
   } else {
     OP(lgb_op_data_arrange(d, c->stream));
     TRY(ensure_pools(c));
+    TRY(ensure_records(c));
     /* membership changed: every patch must be set up again */
     CU(cudaMemsetAsync(d->setup, 0, sizeof(int) * (size_t)d->g.nnodes, c->stream));
     CU(cudaMemsetAsync(d->solved, 0, sizeof(int) * (size_t)d->g.nnodes, c->stream));
@@ -596,6 +651,46 @@ static int fill_data(lgb_ctx *c, int n, const double *coords, const double *valu
   }
   CU(cudaStreamSynchronize(c->stream));
   c->data_filled = 1;
+  return 0;
+}
+
+/* Work-unit capacity of the evaluation kernel from the particles-per-cell histogram: the cost of a
+   capacity C = 64m (m = 1..4, R = 2 particles per thread) is, per work unit, one warp-equivalent of
+   block staging plus its active warps plus a third of a warp for each warp left without particles
+   (it still stages and occupies the SM). */
+static int choose_chunk(lgb_ctx *c)
+{
+  lgb_dev *d = &c->d;
+  int nc = d->g.ncells, i, m, best = 4;
+  double bestcost = -1.0;
+  int *cnt = (int *)malloc(sizeof(int) * (size_t)(nc + 1));
+  if (!cnt) return set_error(LAGRBF_ERR_MEM, "out of host memory");
+  CU(cudaMemcpyAsync(cnt, d->pstart, sizeof(int) * (size_t)(nc + 1), cudaMemcpyDeviceToHost, c->stream));
+  CU(cudaStreamSynchronize(c->stream));
+  for (m = 4; m >= 1; m--) {
+    double cost = 0.0;
+    int cap = 64 * m, twarps = 2 * m;
+    for (i = 0; i < nc; i++) {
+      int n = cnt[i + 1] - cnt[i], nch, per, aw;
+      if (n <= 0) continue;
+      nch = (n + cap - 1) / cap;
+      per = (n + nch - 1) / nch;
+      aw = ((per + 1) / 2 + 31) / 32;
+      cost += nch * (1.0 + aw + (twarps - aw) / 3.0);
+    }
+    if (bestcost < 0.0 || cost < bestcost * 0.98) { bestcost = cost; best = m; }
+  }
+  free(cnt);
+  {
+    const char *env = getenv("LAGRBF_CHUNK");
+    if (env && atoi(env) >= 64 && atoi(env) <= LGB_CHUNK_MAX) best = atoi(env) / 64;
+  }
+  if (64 * best != d->chunk_cap) {
+    d->chunk_cap = 64 * best;
+    invalidate_graph(c);
+    OP(lgb_op_bin_particles(d, 0, c->stream)); /* chunk offsets for the new capacity */
+  }
+  d->max_chunks = d->g.ncells + (d->np + d->chunk_cap - 1) / d->chunk_cap + 1;
   return 0;
 }
 
@@ -647,10 +742,7 @@ static int fill_points(lgb_ctx *c, int n, const double *coords, const double *va
     free(ones);
   }
   OP(lgb_op_bin_particles(d, 1, c->stream));
-  {
-    int mc = d->g.ncells + (n + LGB_CHUNK - 1) / LGB_CHUNK + 1;
-    d->max_chunks = mc;
-  }
+  TRY(choose_chunk(c));
   CU(cudaStreamSynchronize(c->stream));
   c->points_filled = 1;
   return 0;
@@ -699,6 +791,7 @@ static int partitions_setup(lgb_ctx *c)
     cudaEventRecord(c->ev[0], c->stream);
   }
   OP(lgb_op_factor(&c->d, c->stream));
+  OP(lgb_op_build_records(&c->d, 0, c->stream));
   if (c->profiling) {
     float ms = 0.f;
     cudaEventRecord(c->ev[1], c->stream);
@@ -738,7 +831,10 @@ static int reset_coefficients(lgb_ctx *c)
 {
   lgb_dev *d = &c->d;
   /* LagRBF_PartitionsReset: A_KSP_ASMB destroys the patch set-ups, the others only the solution */
-  if (d->solve_method == LGB_A_KSP_ASMB) CU(cudaMemsetAsync(d->setup, 0, sizeof(int) * (size_t)d->g.nnodes, c->stream));
+  if (d->solve_method == LGB_A_KSP_ASMB) {
+    CU(cudaMemsetAsync(d->setup, 0, sizeof(int) * (size_t)d->g.nnodes, c->stream));
+    OP(lgb_op_build_records(d, 1, c->stream)); /* not-set-up patches contribute nothing */
+  }
   CU(cudaMemsetAsync(d->solved, 0, sizeof(int) * (size_t)d->g.nnodes, c->stream));
   CU(cudaStreamSynchronize(c->stream));
   return 0;
@@ -858,6 +954,7 @@ static int run_step(lgb_ctx *c, int analytical)
   CU(cudaMemcpyAsync(c->hctrl, c->d.ctrl, sizeof(lgb_ctrl), cudaMemcpyDeviceToHost, c->stream));
   CU(cudaStreamSynchronize(c->stream));
   if (c->hctrl->factor_error) return check_factor_error(c);
+  if (c->hctrl->eval_error) return set_error(LAGRBF_ERR_TIMEOUT, "a bounded wait of the evaluation kernel gave up");
   return 0;
 }
 
@@ -1152,6 +1249,8 @@ LAGRBF_EXPORT int lagrbf_gpu_get_stats(void *ctx, lagrbf_stats_t *st)
   st->max_patch = c->d.max_patch;
   st->npatch_setup = ns;
   st->dt = c->hctrl->dt_adv;
+  st->chunk_cap = c->d.chunk_cap;
+  st->records = c->d.rec32 != NULL;
   return 0;
 }
 

@@ -32,8 +32,9 @@ enum { LGB_RK1 = 0, LGB_RK2 = 1, LGB_RK4 = 2, LGB_DOPRI = 3 };
 enum { LGB_A_FACTOR = 0, LGB_A_KSP = 1, LGB_A_KSP_ASMB = 2 };
 enum { LGB_PREC_FP64 = 0, LGB_PREC_FP32 = 1 };
 
-/* Particles per evaluation work unit (one CTA): 128 threads x 2 particles. */
-#define LGB_CHUNK 256
+/* Largest evaluation work unit (particles of one cell handled by one CTA); the actual capacity
+   (d->chunk_cap, a multiple of 64) is chosen from the particles-per-cell histogram. */
+#define LGB_CHUNK_MAX 256
 
 /* PU mesh geometry (DMDA with Q1 elements): nodes are patches, elements are cells. */
 typedef struct {
@@ -70,6 +71,7 @@ typedef struct {
   int factor_node;     /* patch with that pivot                                    */
   int nfactored;
   double factor_flops;
+  int eval_error;      /* a bounded wait of the evaluation kernel gave up */
 } lgb_ctrl;
 
 typedef struct {
@@ -100,6 +102,12 @@ typedef struct {
   double *xp, *fields, *vel, *x0, *vadv;
   int *cell_p, *alive, *pcount, *pstart, *pfill, *plist, *chunk_start;
   int max_chunks;
+  int chunk_cap;       /* particles per evaluation work unit */
+  /* precomputed FP32 record blocks streamed by TMA (NULL: gather staging) */
+  float *rec32;
+  long long *rec_off;
+  long long rec_cap;
+  int rec_fp;          /* fields per record (= dim) */
   /* scratch for scans */
   int *scan_tmp;
   long long *scan_tmp64;
@@ -125,6 +133,7 @@ int lgb_op_factor(lgb_dev *d, void *stream);            /* set up / solve queued
 /* lgb_eval.cu */
 int lgb_op_eval(lgb_dev *d, int nf_first, int nf, double *out, int out_stride, void *stream);
 int lgb_op_weights(lgb_dev *d, double *w, void *stream);
+int lgb_op_build_records(lgb_dev *d, int force, void *stream);
 /* lgb_step.cu */
 int lgb_op_stage(lgb_dev *d, int scheme, int stage, void *stream);
 int lgb_op_dopri_error(lgb_dev *d, void *stream);
