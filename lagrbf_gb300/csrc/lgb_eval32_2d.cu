@@ -2,21 +2,29 @@
  * lgb_eval32_2d.cu -- FP32-evaluation instantiations of the PU evaluation kernel (lgb_eval.cuh), 2D.
  */
 #include "lgb_eval.cuh"
+#include <stdlib.h>
 
-template <int DIM, int FP, int KER, int STAGE>
-static int launch32(const EvalParams &P, int grid, cudaStream_t s)
+template <int DIM, int FP, int KER, int STAGE, int R>
+static int launch32r(const EvalParams &P, int grid, cudaStream_t s)
 {
   static bool attr = false;
   const int nbuf = (STAGE == 1) ? 2 : 1;
-  /* staging buffer(s) + per-thread running sums of the NEN*FP per-patch partial sums */
-  size_t smem = ((size_t)nbuf * P.budget + (size_t)(2 * (1 << DIM) * FP + 1) * (P.chunk_cap / 2)) * sizeof(float);
+  /* staging buffer(s) + per-thread running sums of the R*NEN*FP per-patch partial sums */
+  size_t smem = ((size_t)nbuf * P.budget + (size_t)(R * (1 << DIM) * FP + 1) * (P.chunk_cap / R)) * sizeof(float);
   if (!attr) {
-    size_t smax = ((size_t)nbuf * P.budget + (size_t)(2 * (1 << DIM) * FP + 1) * (LGB_CHUNK_MAX / 2)) * sizeof(float);
-    cudaFuncSetAttribute(k_eval<float, DIM, FP, 2, KER, STAGE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smax);
+    size_t smax = ((size_t)nbuf * P.budget + (size_t)(R * (1 << DIM) * FP + 1) * (LGB_CHUNK_MAX / R)) * sizeof(float);
+    cudaFuncSetAttribute(k_eval<float, DIM, FP, R, KER, STAGE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smax);
     attr = true;
   }
-  k_eval<float, DIM, FP, 2, KER, STAGE><<<grid, P.chunk_cap / 2, smem, s>>>(P);
+  k_eval<float, DIM, FP, R, KER, STAGE><<<grid, P.chunk_cap / R, smem, s>>>(P);
   return (int)cudaGetLastError();
+}
+
+/* Two particles per thread (four per thread measured slower: fewer active lanes per work unit). */
+template <int DIM, int FP, int KER, int STAGE>
+static int launch32(const EvalParams &P, int grid, cudaStream_t s)
+{
+  return launch32r<DIM, FP, KER, STAGE, 2>(P, grid, s);
 }
 
 template <int DIM, int KER>

@@ -4,16 +4,17 @@
  */
 #include "lgb_eval.cuh"
 #include <string.h>
+#include <stdlib.h>
 
 extern "C" int lgb_eval32_launch_3d(const EvalParams *P, int fp, int ker, int stage, int grid, void *stream);
 extern "C" int lgb_eval32_launch_2d(const EvalParams *P, int fp, int ker, int stage, int grid, void *stream);
 extern "C" int lgb_build_records_3d(const EvalParams *P, int force, int grid, void *stream);
 extern "C" int lgb_build_records_2d(const EvalParams *P, int force, int grid, void *stream);
 
-/* Staging budgets (elements): FP32 gather 30 KB, FP32 TMA 2 x 16 KB (each + up to 32 KB of running
-   sums: four CTAs per SM), FP64 48 KB. */
+/* Staging budgets (elements): FP32 gather 30 KB, FP32 TMA 2 x 12 KB (each + the running sums:
+   four to five CTAs per SM; measured best among 4/6/8/12/14/16 KB rings), FP64 48 KB. */
 #define BUDGET32 7680
-#define BUDGET32_TMA 3584
+#define BUDGET32_TMA 3072
 #define BUDGET64 6144
 
 template <int DIM, int FP>
@@ -39,6 +40,16 @@ static int launch64_fp(const EvalParams &P, int fp, int grid, cudaStream_t s)
   case 3: return launch64<DIM, 3>(P, grid, s);
   default: return launch64<DIM, 4>(P, grid, s);
   }
+}
+
+static int tma_budget(void)
+{
+  static int b = -1;
+  if (b < 0) {
+    const char *e = getenv("LAGRBF_TMA_BUDGET");
+    b = (e && atoi(e) >= 256) ? (atoi(e) / 4) * 4 : BUDGET32_TMA;
+  }
+  return b;
 }
 
 /* Evaluate fields [nf_first, nf_first+nf) of the coefficient pool at every live particle and
@@ -78,7 +89,7 @@ extern "C" int lgb_op_eval(lgb_dev *d, int nf_first, int nf, double *out, int ou
     int rc;
     if (d->prec == LGB_PREC_FP32) {
       const int stage = (d->rec32 && f == 0 && fp == g.dim && d->rec_fp == g.dim) ? 1 : 0;
-      P.budget = stage ? BUDGET32_TMA : BUDGET32;
+      P.budget = stage ? tma_budget() : BUDGET32;
       rc = (g.dim == 3) ? lgb_eval32_launch_3d(&P, fp, ker, stage, grid, stream)
                         : lgb_eval32_launch_2d(&P, fp, ker, stage, grid, stream);
     } else {
