@@ -149,6 +149,23 @@ LAGRBF_EXPORT int64_t lagrbf_gpu_get_block_csr(void *ctx, int32_t *blk_start, in
 /* Geometry of the context: dim, n[3], nnodes, ncells, nen and eps_w, eps_r. */
 LAGRBF_EXPORT int lagrbf_gpu_get_geometry(void *ctx, int32_t *ints /* 7 */, double *reals /* 2 */);
 
+/* Binning without device allocation (no counterpart in the reference).  For callers that may not
+   have a library allocate device memory at this point: a code running its time loop from a device
+   pool reserved at start-up, or one recording its step into its own stream capture.  Bins npoints
+   points (coords: device, npoints*dim doubles) into the cells of the uniform mesh of nodes[dim]
+   nodes over [O, L], as the context path does: cellid[i] (device, npoints) is the cell or -1 when
+   outside; cell_start (device, ncells+1) the exclusive scan of the per-cell counts; order (device,
+   npoints, first cell_start[ncells] entries valid) the point indices by cell, input order within a
+   cell.  All scratch is a static device array of this library sized for at most
+   LAGRBF_NOALLOC_MAX_CELLS cells; larger meshes are rejected with LAGRBF_ERR_ARG_OUTOFRANGE.
+   Asynchronous on `stream` (cudaStream_t, NULL = legacy default stream).  The first call on a device
+   (that device current) resolves the scratch address, so it should precede any stream capture.
+   Calls that overlap on one device share the scratch and race: keep them on one stream. */
+#define LAGRBF_NOALLOC_MAX_CELLS (1 << 20)
+LAGRBF_EXPORT int lagrbf_gpu_bin_points_noalloc(int32_t dim, const int32_t *nodes, const double *O, const double *L,
+                                                int32_t npoints, const double *coords, int32_t *cellid,
+                                                int32_t *cell_start, int32_t *order, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -15,7 +15,8 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "liblagrbf.so")
 
-CU_SOURCES = ["lgb_bin.cu", "lgb_eval32_3d.cu", "lgb_eval32_2d.cu", "lgb_eval64.cu", "lgb_factor.cu", "lgb_step.cu"]
+CU_SOURCES = ["lgb_bin.cu", "lgb_eval32_3d.cu", "lgb_eval32_2d.cu", "lgb_eval64.cu", "lgb_factor.cu", "lgb_step.cu",
+              "lgb_noalloc.cu"]
 C_SOURCES = ["lgb_host.c"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

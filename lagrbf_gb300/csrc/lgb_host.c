@@ -48,6 +48,8 @@ static int set_error(int code, const char *fmt, ...)
 
 LAGRBF_EXPORT const char *lagrbf_gpu_last_error(void) { return g_errmsg; }
 
+int lgb_set_error_msg(int code, const char *msg) { return set_error(code, "%s", msg); }
+
 #define CU(call)                                                                                    \
   do {                                                                                              \
     cudaError_t e_ = (call);                                                                        \

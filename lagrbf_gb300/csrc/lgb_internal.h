@@ -142,6 +142,8 @@ enum { LGB_CTRL_BEGIN_STEP = 0, LGB_CTRL_END_STEP = 1, LGB_CTRL_RESET_CFL = 2, L
 int lgb_op_copy_velocity(lgb_dev *d, void *stream);     /* vel <- fields[:, :dim] */
 int lgb_op_count_alive(lgb_dev *d, void *stream);
 int lgb_device_info(int *nsm, int *smem_optin);
+/* Sets the calling thread's error message (returned by lagrbf_gpu_last_error); returns code. */
+int lgb_set_error_msg(int code, const char *msg);
 long long lgb_launch_count(void);
 
 #ifdef __cplusplus
