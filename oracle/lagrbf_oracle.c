@@ -155,6 +155,8 @@ static inline double phi_lane(int kernel, double r, double eps)
   }
 }
 
+double orc_phi_lane(int kernel, double r, double eps) { return phi_lane(kernel, r, eps); }
+
 /* ======================================================================================= */
 /* binning                                                                                  */
 /* ======================================================================================= */
@@ -373,6 +375,11 @@ static void assemble(const orc_pu *pu, int kernel, int m, const int *idx, const 
       if (i != j) A[(size_t)m * j + i] = v;
     }
   }
+}
+
+void orc_assemble(const orc_pu *pu, int kernel, int m, const int *idx, const double *coords, double *A)
+{
+  assemble(pu, kernel, m, idx, coords, A);
 }
 
 /* Lower Cholesky in place (row-major, lower triangle used); left-looking, ascending-k dot

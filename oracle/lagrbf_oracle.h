@@ -59,6 +59,8 @@ typedef struct {
 void   orc_pu_setup(orc_pu *pu, const orc_config *cfg);
 /* kernels_rbf.c:31-91 */
 double orc_phi_scalar(int kernel, double r, double eps);
+/* One lane of the vector kernels (kernels_rbf_avx512.h:34-95, kernels_rbf_avx.h:35-94 op order). */
+double orc_phi_lane(int kernel, double r, double eps);
 /* Q1 corner k of cell `cell` (PETSc DMDAGetElements node order). */
 int    orc_cell_corner(const orc_pu *pu, int cell, int k);
 
@@ -82,6 +84,7 @@ void orc_weights(const orc_pu *pu, int np, const double *coords, const int *cell
 /* Assemble (partition_asmb_avx512.c:119-198), Cholesky (LAPACK potrf semantics) and solve
    (partition_factor.c:57-135).  coeffs is column-major [f*m + j].  Returns 0, or the 1-based
    row of a non-positive pivot. */
+void orc_assemble(const orc_pu *pu, int kernel, int m, const int *idx, const double *coords, double *A);
 int orc_patch_solve(const orc_pu *pu, int kernel, int m, const int *idx, const double *coords,
                     int nfields, const double *values, double *coeffs);
 

@@ -26,6 +26,14 @@ class OrcConfig(ctypes.Structure):
     ]
 
 
+class OrcPU(ctypes.Structure):
+    _fields_ = [
+        ("dim", ctypes.c_int), ("n", ctypes.c_int * 3), ("nnodes", ctypes.c_int), ("ncells", ctypes.c_int),
+        ("nen", ctypes.c_int), ("O", ctypes.c_double * 3), ("L", ctypes.c_double * 3), ("h", ctypes.c_double * 3),
+        ("eps_w", ctypes.c_double), ("eps_r", ctypes.c_double),
+    ]
+
+
 VFN_BATCH = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_int32, ctypes.c_int32, ctypes.POINTER(ctypes.c_double),
                              ctypes.POINTER(ctypes.c_double), ctypes.c_void_p)
 
@@ -84,6 +92,23 @@ def lib():
         L.orc_time_baseline.argtypes = [ctypes.POINTER(OrcConfig), ctypes.c_int, d, d, ctypes.c_int, d, ctypes.c_int,
                                         ctypes.c_double, ctypes.c_int, ctypes.POINTER(ctypes.c_double),
                                         ctypes.POINTER(ctypes.c_double)]
+        pu = ctypes.POINTER(OrcPU)
+        L.orc_pu_setup.argtypes = [pu, ctypes.POINTER(OrcConfig)]
+        L.orc_phi_scalar.restype = ctypes.c_double
+        L.orc_phi_scalar.argtypes = [ctypes.c_int, ctypes.c_double, ctypes.c_double]
+        L.orc_phi_lane.restype = ctypes.c_double
+        L.orc_phi_lane.argtypes = [ctypes.c_int, ctypes.c_double, ctypes.c_double]
+        L.orc_locate.argtypes = [pu, ctypes.c_int, d, i]
+        L.orc_cell_csr.argtypes = [pu, ctypes.c_int, i, i, i]
+        L.orc_patch_csr.restype = ctypes.c_long
+        L.orc_patch_csr.argtypes = [pu, i, i, IN, IN]
+        L.orc_block_csr.restype = ctypes.c_long
+        L.orc_block_csr.argtypes = [pu, i, i, IN, IN]
+        L.orc_weights.argtypes = [pu, ctypes.c_int, d, i, IN, d]
+        L.orc_assemble.argtypes = [pu, ctypes.c_int, ctypes.c_int, i, d, d]
+        L.orc_patch_solve.argtypes = [pu, ctypes.c_int, ctypes.c_int, i, d, ctypes.c_int, d, d]
+        L.orc_eval.argtypes = [pu, ctypes.c_int, ctypes.c_int, d, i, IN, d, d, i, i, i, i, IN,
+                               ctypes.POINTER(ctypes.POINTER(ctypes.c_double)), ctypes.c_int, d]
         _lib = L
     return _lib
 
@@ -180,3 +205,81 @@ class Oracle:
         p = np.zeros(max(tot, 1), dtype=np.int32)
         lib().orc_get_block_csr(self.h, s, p)
         return s, p[:tot]
+
+
+class Pieces:
+    """The oracle's building blocks on one mesh (geometry, binning, membership, weights, patch
+    solves and evaluation), for comparisons below the lagrbf_* API."""
+
+    def __init__(self, **kw):
+        self.cfg = make_config(**kw)
+        self.pu = OrcPU()
+        lib().orc_pu_setup(ctypes.byref(self.pu), ctypes.byref(self.cfg))
+        self.dim, self.nen = self.pu.dim, self.pu.nen
+        self.nnodes, self.ncells = self.pu.nnodes, self.pu.ncells
+
+    def locate(self, x):
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        c = np.zeros(len(x), dtype=np.int32)
+        lib().orc_locate(ctypes.byref(self.pu), len(x), x.reshape(-1), c)
+        return c
+
+    def csr(self, cellid):
+        cs = np.zeros(self.ncells + 1, dtype=np.int32)
+        cp = np.zeros(max(len(cellid), 1), dtype=np.int32)
+        lib().orc_cell_csr(ctypes.byref(self.pu), len(cellid), cellid, cs, cp)
+        tot = lib().orc_patch_csr(ctypes.byref(self.pu), cs, cp, None, None)
+        ps = np.zeros(self.nnodes + 1, dtype=np.int32)
+        pp = np.zeros(max(tot, 1), dtype=np.int32)
+        lib().orc_patch_csr(ctypes.byref(self.pu), cs, cp, ps, pp)
+        tot = lib().orc_block_csr(ctypes.byref(self.pu), cs, cp, None, None)
+        bs = np.zeros(self.ncells + 1, dtype=np.int32)
+        bp = np.zeros(max(tot, 1), dtype=np.int32)
+        lib().orc_block_csr(ctypes.byref(self.pu), cs, cp, bs, bp)
+        return (cs, cp), (ps, pp), (bs, bp)
+
+    def weights(self, x, cellid):
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        w = np.zeros(len(x) * self.nen)
+        lib().orc_weights(ctypes.byref(self.pu), len(x), x.reshape(-1), cellid, None, w)
+        return w.reshape(len(x), self.nen)
+
+    def assemble(self, kernel, idx, xd):
+        m = len(idx)
+        A = np.zeros(m * m)
+        lib().orc_assemble(ctypes.byref(self.pu), kernel, m, np.ascontiguousarray(idx, dtype=np.int32),
+                           np.ascontiguousarray(xd, dtype=np.float64).reshape(-1), A)
+        return A.reshape(m, m)
+
+    def solve_all(self, kernel, xd, fd, ps, pp):
+        """Coefficients of every patch, packed column-major per patch; offsets coff[nnodes+1]."""
+        nf = fd.shape[1]
+        sizes = np.diff(ps).astype(np.int64)
+        coff = np.concatenate([[0], np.cumsum(sizes * nf)]).astype(np.int64)
+        coeffs = np.zeros(max(int(coff[-1]), 1))
+        xdf = np.ascontiguousarray(xd, dtype=np.float64).reshape(-1)
+        fdf = np.ascontiguousarray(fd, dtype=np.float64).reshape(-1)
+        for k in range(self.nnodes):
+            m = int(sizes[k])
+            if m == 0:
+                continue
+            out = np.zeros(m * nf)
+            rc = lib().orc_patch_solve(ctypes.byref(self.pu), kernel, m, np.ascontiguousarray(pp[ps[k]:ps[k + 1]]),
+                                       xdf, nf, fdf, out)
+            if rc:
+                raise RuntimeError("patch %d: non-positive pivot at row %d" % (k, rc))
+            coeffs[coff[k]:coff[k + 1]] = out
+        return coeffs, coff
+
+    def eval(self, kernel, xp, cellid, w, xd, bs, bp, ps, pp, coeffs, coff, nf_total, nf):
+        n = len(xp)
+        ptrs = (ctypes.POINTER(ctypes.c_double) * self.nnodes)()
+        base = coeffs.ctypes.data
+        for k in range(self.nnodes):
+            ptrs[k] = ctypes.cast(base + 8 * int(coff[k]), ctypes.POINTER(ctypes.c_double))
+        setup = np.ones(self.nnodes, dtype=np.int32)
+        out = np.zeros(n * nf)
+        lib().orc_eval(ctypes.byref(self.pu), kernel, n, np.ascontiguousarray(xp, dtype=np.float64).reshape(-1),
+                       cellid, None, np.ascontiguousarray(w).reshape(-1),
+                       np.ascontiguousarray(xd, dtype=np.float64).reshape(-1), bs, bp, ps, pp, setup, ptrs, nf, out)
+        return out.reshape(n, nf)
