@@ -49,6 +49,8 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--profile-only", action="store_true", help="setup + a few steps, for ncu")
     ap.add_argument("--quick", action="store_true", help="only the FP32 timed loop and the roofline pass")
+    ap.add_argument("--solve-method", type=int, default=1,
+                    help="1: A_KSP (factors resident), 2: A_KSP_ASMB (re-factor, no factor storage)")
     return ap.parse_args()
 
 
@@ -93,6 +95,19 @@ class ClockSampler:
                           and "Not" not in s[3 + i]})
         return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
                 "reasons": reasons, "samples": len(self.samples)}
+
+
+def eval_traffic_per_particle():
+    """DRAM bytes (read + write) per particle of one evaluation launch, from the committed ncu
+    capture of the evaluation kernel (profiles/k_eval_traffic.txt), or None."""
+    p = os.path.join(ROOT, "profiles", "k_eval_traffic.txt")
+    if not os.path.exists(p):
+        return None, None
+    with open(p) as f:
+        for line in f:
+            if line.startswith("dram_bytes_per_particle:"):
+                return float(line.split(":", 1)[1]), "profiles/k_eval_traffic.txt"
+    return None, None
 
 
 def peaks():
@@ -194,7 +209,8 @@ def main():
     cf = L.load_cfuncs()
     xd, fd, xp, opts = workload(args, rank)
     npart = len(xp)
-    ctx = L.LagRBFCtx(**opts, advection=True, advection_scheme=2, advection_cfl=0.3, dt=DT, solve_method=1,
+    ctx = L.LagRBFCtx(**opts, advection=True, advection_scheme=2, advection_cfl=0.3, dt=DT,
+                      solve_method=args.solve_method,
                       eval_precision="fp32", cuda_device=local)
     # ---------------- setup (not timed in `value`) ----------------
     t0 = time.perf_counter()
@@ -248,8 +264,13 @@ def main():
     fp32_peak = cf["lagrbf_gpu_fp32_peak_tflops"]()
     eval_tflops = sp["eval_flops"] / (sp["eval_ms"] * 1e-3) / 1e12 if sp["eval_ms"] > 0 else 0.0
     eval_gbs = sp["eval_bytes"] / (sp["eval_ms"] * 1e-3) / 1e9 if sp["eval_ms"] > 0 else 0.0
+    tpp, tsrc = eval_traffic_per_particle()
+    traffic = tpp * sp["np_alive"] if tpp else None
     roofline = {"bound": "fp32", "achieved": eval_tflops, "peak": fp32_peak, "unit": "TFLOP/s",
-                "frac": eval_tflops / fp32_peak if fp32_peak > 0 else None, "traffic": None,
+                "frac": eval_tflops / fp32_peak if fp32_peak > 0 else None, "traffic": traffic,
+                "traffic_source": ("ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch on a smaller "
+                                   "case with the same per-cell densities, per particle, times this launch's "
+                                   "particles (%s)" % tsrc) if tsrc else None,
                 "kernel": "k_eval<float,3,3,2,KER_C2> (PU evaluation)",
                 "peak_source": "measured: FFMA-chain probe on this GPU in this run (lagrbf_gpu_fp32_peak_tflops)",
                 "per_launch_ms": sp["eval_ms"] / max(sp["eval_launches"], 1),
@@ -331,7 +352,8 @@ def main():
             "config": {"workload": "abc3d: %d^3 jittered lattice (%d nodes), ABC flow, %d^3 PU patches, Wendland C2, "
                                    "%d particles/GPU, RK4 dt=%g" % (args.nlat, len(xd), args.npu, args.np, DT),
                        "eval": "FP32 evaluation, FP64 factorisation and weight normalisation",
-                       "solve_method": "A_KSP (factors resident)",
+                       "solve_method": {1: "A_KSP (factors resident)", 2: "A_KSP_ASMB (re-factor per solve)"}
+                       .get(args.solve_method, str(args.solve_method)),
                        "l2": "inputs larger than L2 (particle state %.1f GB)" % (npart * 8 * 3 * 12 / 1e9),
                        "parallelism": "replicas x%d (particles sharded, data replicated)" % world,
                        "setup_s": setup_s, "patches_factored": st0["patches_factored"],
