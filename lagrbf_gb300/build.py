@@ -19,6 +19,8 @@ CU_SOURCES = ["lgb_bin.cu", "lgb_eval32_3d.cu", "lgb_eval32_2d.cu", "lgb_eval64.
               "lgb_noalloc.cu"]
 C_SOURCES = ["lgb_host.c"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+# extra nvcc flags for tuning builds, e.g. LAGRBF_NVCC_FLAGS="-DLGB_X2_UNROLL=2" (default: none)
+EXTRA = os.environ.get("LAGRBF_NVCC_FLAGS", "").split()
 
 
 def _cuda_home():
@@ -57,7 +59,7 @@ def build(verbose=False, force=False):
         o = os.path.join(BUILD, src + ".o")
         objs.append(o)
         if force or _stale(o, [s] + headers):
-            jobs.append([nvcc, "-std=c++17", "-O3", "-lineinfo", *ARCH, "-Xcompiler", "-fPIC",
+            jobs.append([nvcc, "-std=c++17", "-O3", "-lineinfo", *ARCH, "-Xcompiler", "-fPIC", *EXTRA,
                          "-Xptxas", "-v" if verbose else "-O3", "-c", s, "-o", o])
     for src in C_SOURCES:
         s = os.path.join(CSRC, src)

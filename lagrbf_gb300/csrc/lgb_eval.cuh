@@ -92,8 +92,13 @@ __host__ __device__ constexpr int eslot(int dim, int k, int o)
    to a 16-byte multiple. */
 template <typename Real> __host__ __device__ constexpr int erec(int ninv, int fp)
 {
-  return sizeof(Real) == 4 ? ((4 + ninv * fp + 3) / 4) * 4 : ((4 + ninv * fp + 1) / 2) * 2;
+  return sizeof(Real) == 4 ? LGB_REC32_LEN(ninv, fp) : ((4 + ninv * fp + 1) / 2) * 2;
 }
+/* Record layout: coordinate d at rec[d * EXS], coefficient (field f, patch j) at
+   rec[EHEAD + (f * ninv + j) * EDUP] (FP64 records: {x, y, z, 0} and single coefficients). */
+template <typename Real> __host__ __device__ constexpr int ehead() { return sizeof(Real) == 4 ? LGB_REC32_HEAD : 4; }
+template <typename Real> __host__ __device__ constexpr int edup() { return sizeof(Real) == 4 ? LGB_REC32_DUP : 1; }
+template <typename Real> __host__ __device__ constexpr int exs() { return sizeof(Real) == 4 ? 2 : 1; }
 
 template <typename Real, int KER>
 __device__ __forceinline__ Real eval_phi(Real d2, Real eps, Real ga, int kernel)
@@ -108,6 +113,183 @@ __device__ __forceinline__ Real eval_phi(Real d2, Real eps, Real ga, int kernel)
     return exp2f(ga * d2);
   } else {
     return lgb_phi<Real>(kernel, sqrt(d2), eps);
+  }
+}
+
+#define LGB_PRAGMA(x) _Pragma(#x)
+#define LGB_UNROLL(n) LGB_PRAGMA(unroll n)
+#ifndef LGB_X2_UNROLL
+#define LGB_X2_UNROLL 2 /* points of a segment in flight per thread in the packed FP32 loop */
+#endif
+
+/* ---- packed FP32 pairs (PTX .f32x2, sm_100 and later): one instruction applies the IEEE
+   single-precision operation to both halves of a 64-bit register pair ---- */
+typedef unsigned long long f32x2;
+__device__ __forceinline__ f32x2 x2_pack(float a, float b)
+{
+  f32x2 r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+  return r;
+}
+__device__ __forceinline__ void x2_unpack(f32x2 v, float &a, float &b)
+{
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(v));
+}
+__device__ __forceinline__ f32x2 x2_fma(f32x2 a, f32x2 b, f32x2 c)
+{
+  f32x2 d;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+  return d;
+}
+__device__ __forceinline__ f32x2 x2_mul(f32x2 a, f32x2 b)
+{
+  f32x2 d;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ f32x2 x2_sub(f32x2 a, f32x2 b)
+{
+  f32x2 d;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+
+/* index of the j-th set bit of mask (the corner of the j-th involved patch) */
+__host__ __device__ constexpr int ekj(int mask, int j)
+{
+  for (int k = 0; k < 8; k++)
+    if ((mask >> k) & 1) {
+      if (j == 0) return k;
+      --j;
+    }
+  return 0;
+}
+
+/* FP32 segment with two particles per thread on packed pairs: the distances and the Wendland C2
+   polynomial run on (particle 0, particle 1) pairs against the record's duplicated coordinates.
+   With duplicated coefficients (LGB_REC32_DUP == 2) the sums also run on particle pairs; otherwise
+   on (patch 2i, patch 2i+1) pairs of one field.  Each lane performs the same IEEE operations in the
+   same order as the scalar form, so the results are identical to it.  Partial sums of the segment
+   go to the running sums at the end (blocked accumulation). */
+template <int DIM, int FP, int KER, int NI>
+__device__ __forceinline__ void eval_segment_x2(const float *__restrict__ rec, int n, const float (&px)[2][3], float eps,
+                                                float ga, float *__restrict__ run, int mask)
+{
+  constexpr int NEN = EGeo<DIM>::NEN;
+  constexpr int H = LGB_REC32_HEAD;
+  constexpr int S = erec<float>(NI, FP);
+  constexpr int NV = S / 4;
+  constexpr bool DUP = (LGB_REC32_DUP == 2);
+  constexpr int NP = DUP ? NI : NI / 2;     /* accumulator pairs per field */
+  constexpr bool ODD = !DUP && (NI & 1);    /* one unpaired patch (NI == 1) */
+  const f32x2 pxx = x2_pack(px[0][0], px[1][0]), pyy = x2_pack(px[0][1], px[1][1]);
+  const f32x2 pzz = x2_pack(px[0][2], px[1][2]);
+  const f32x2 neps = x2_pack(-eps, -eps), one = x2_pack(1.f, 1.f), m4 = x2_pack(-4.f, -4.f), five = x2_pack(5.f, 5.f);
+  f32x2 ap[FP][NP > 0 ? NP : 1];    /* DUP: lanes = particles; else lanes = patches, particle 0 */
+  f32x2 bp[FP][(!DUP && NP > 0) ? NP : 1]; /* !DUP: particle 1 */
+  float as[2][FP];
+#pragma unroll
+  for (int f = 0; f < FP; f++) {
+    as[0][f] = 0.f;
+    as[1][f] = 0.f;
+#pragma unroll
+    for (int q = 0; q < (NP > 0 ? NP : 1); q++) ap[f][q] = 0ull;
+#pragma unroll
+    for (int q = 0; q < ((!DUP && NP > 0) ? NP : 1); q++) bp[f][q] = 0ull;
+  }
+  LGB_UNROLL(LGB_X2_UNROLL)
+  for (int p = 0; p < n; ++p) {
+    float v[S];
+    const float4 *rv = reinterpret_cast<const float4 *>(rec + (size_t)p * S);
+#pragma unroll
+    for (int q = 0; q < NV; q++) {
+      const float4 t = rv[q];
+      v[4 * q + 0] = t.x; v[4 * q + 1] = t.y; v[4 * q + 2] = t.z; v[4 * q + 3] = t.w;
+    }
+    const f32x2 dx = x2_sub(pxx, x2_pack(v[0], v[1]));
+    const f32x2 dy = x2_sub(pyy, x2_pack(v[2], v[3]));
+    f32x2 d2;
+    if constexpr (DIM == 3) {
+      const f32x2 dz = x2_sub(pzz, x2_pack(v[4], v[5]));
+      d2 = x2_fma(dx, dx, x2_fma(dy, dy, x2_mul(dz, dz)));
+    } else {
+      d2 = x2_fma(dx, dx, x2_mul(dy, dy));
+    }
+    float d2a, d2b;
+    x2_unpack(d2, d2a, d2b);
+    f32x2 ph;
+    if constexpr (KER == KER_C2) {
+      float ra, rb;
+      asm("sqrt.approx.f32 %0, %1;" : "=f"(ra) : "f"(d2a));
+      asm("sqrt.approx.f32 %0, %1;" : "=f"(rb) : "f"(d2b));
+      float ua, ub;
+      x2_unpack(x2_fma(x2_pack(ra, rb), neps, one), ua, ub); /* 1 - eps*r */
+      const f32x2 u = x2_pack(fmaxf(ua, 0.f), fmaxf(ub, 0.f));
+      const f32x2 u2 = x2_mul(u, u);
+      ph = x2_mul(x2_mul(u2, u2), x2_fma(u, m4, five));
+    } else {
+      ph = x2_pack(exp2f(ga * d2a), exp2f(ga * d2b));
+    }
+    if constexpr (DUP) {
+#pragma unroll
+      for (int f = 0; f < FP; f++)
+#pragma unroll
+        for (int j = 0; j < NI; j++)
+          ap[f][j] = x2_fma(ph, x2_pack(v[H + 2 * (f * NI + j)], v[H + 2 * (f * NI + j) + 1]), ap[f][j]);
+    } else {
+      float pa, pb;
+      x2_unpack(ph, pa, pb);
+      const f32x2 PA = x2_pack(pa, pa), PB = x2_pack(pb, pb);
+#pragma unroll
+      for (int f = 0; f < FP; f++) {
+#pragma unroll
+        for (int q = 0; q < NP; q++) {
+          const f32x2 c = x2_pack(v[H + f * NI + 2 * q], v[H + f * NI + 2 * q + 1]);
+          ap[f][q] = x2_fma(PA, c, ap[f][q]);
+          bp[f][q] = x2_fma(PB, c, bp[f][q]);
+        }
+        if constexpr (ODD) {
+          const float c = v[H + f * NI + NI - 1];
+          as[0][f] = fmaf(pa, c, as[0][f]);
+          as[1][f] = fmaf(pb, c, as[1][f]);
+        }
+      }
+    }
+  }
+  /* corners of the involved patches, in record order (ascending corner index) */
+  int kj[NI];
+  unsigned m = (unsigned)mask;
+#pragma unroll
+  for (int j = 0; j < NI; j++) {
+    kj[j] = __ffs(m) - 1;
+    m &= m - 1;
+  }
+#pragma unroll
+  for (int f = 0; f < FP; f++) {
+    if constexpr (DUP) {
+#pragma unroll
+      for (int j = 0; j < NI; j++) {
+        float a, b;
+        x2_unpack(ap[f][j], a, b);
+        run[(0 * NEN + kj[j]) * FP + f] += a;
+        run[(1 * NEN + kj[j]) * FP + f] += b;
+      }
+    } else {
+#pragma unroll
+      for (int q = 0; q < NP; q++) {
+        float lo, hi;
+        x2_unpack(ap[f][q], lo, hi);
+        run[(0 * NEN + kj[2 * q]) * FP + f] += lo;
+        run[(0 * NEN + kj[2 * q + 1]) * FP + f] += hi;
+        x2_unpack(bp[f][q], lo, hi);
+        run[(1 * NEN + kj[2 * q]) * FP + f] += lo;
+        run[(1 * NEN + kj[2 * q + 1]) * FP + f] += hi;
+      }
+      if constexpr (ODD) {
+        run[(0 * NEN + kj[NI - 1]) * FP + f] += as[0][f];
+        run[(1 * NEN + kj[NI - 1]) * FP + f] += as[1][f];
+      }
+    }
   }
 }
 
@@ -141,9 +323,9 @@ __device__ __forceinline__ void eval_segment(const Real *__restrict__ rec, int n
     Real phi[R];
 #pragma unroll
     for (int r = 0; r < R; r++) {
-      Real dx = px[r][0] - v[0], dy = px[r][1] - v[1], d2;
+      Real dx = px[r][0] - v[0], dy = px[r][1] - v[exs<Real>()], d2;
       if constexpr (DIM == 3) {
-        Real dz = px[r][2] - v[2];
+        Real dz = px[r][2] - v[2 * exs<Real>()];
         d2 = fma(dx, dx, fma(dy, dy, dz * dz));
       } else {
         d2 = fma(dx, dx, dy * dy);
@@ -156,7 +338,7 @@ __device__ __forceinline__ void eval_segment(const Real *__restrict__ rec, int n
       if ((MASK >> k) & 1) {
 #pragma unroll
         for (int f = 0; f < FP; f++) {
-          Real cf = v[4 + j * FP + f];
+          Real cf = v[ehead<Real>() + (f * NI + j) * edup<Real>()];
 #pragma unroll
           for (int r = 0; r < R; r++) acc[r][k][f] = fma(phi[r], cf, acc[r][k][f]);
         }
@@ -190,7 +372,20 @@ __device__ __forceinline__ void eval_dispatch(int o, const Real *rec, int n, con
                                               float *run, int rstride)
 {
 #define EV_CASE(OO) case OO: eval_segment<Real, DIM, FP, R, KER, OO>(rec, n, px, acc, eps, ga, kernel, run, rstride); break;
-  if constexpr (DIM == 3) {
+  if constexpr (sizeof(Real) == 4 && R == 2 && (KER == KER_C2 || KER == KER_GAUSS)) {
+    /* packed FP32 path: one code body per number of involved patches (1, 2, 4 or 8), the corner
+       mapping is applied when the segment's sums are flushed */
+    const float *rf = reinterpret_cast<const float *>(rec);
+    const float(&pf)[2][3] = reinterpret_cast<const float(&)[2][3]>(px);
+    const int mask = einv_mask(DIM, o);
+    switch (epopc(mask)) {
+    case 1: eval_segment_x2<DIM, FP, KER, 1>(rf, n, pf, (float)eps, (float)ga, run, mask); break;
+    case 2: eval_segment_x2<DIM, FP, KER, 2>(rf, n, pf, (float)eps, (float)ga, run, mask); break;
+    case 4: eval_segment_x2<DIM, FP, KER, 4>(rf, n, pf, (float)eps, (float)ga, run, mask); break;
+    case 8: if constexpr (DIM == 3) eval_segment_x2<DIM, FP, KER, 8>(rf, n, pf, (float)eps, (float)ga, run, mask); break;
+    default: break;
+    }
+  } else if constexpr (DIM == 3) {
     switch (o) {
       EV_CASE(0) EV_CASE(1) EV_CASE(2) EV_CASE(3) EV_CASE(4) EV_CASE(5) EV_CASE(6) EV_CASE(7) EV_CASE(8)
       EV_CASE(9) EV_CASE(10) EV_CASE(11) EV_CASE(12) EV_CASE(13) EV_CASE(14) EV_CASE(15) EV_CASE(16)
@@ -297,33 +492,38 @@ __device__ __forceinline__ void write_record(const EvalParams &P, int o, int pp,
   const int S = erec<Real>(epopc(mask), FP);
   if constexpr (sizeof(Real) == 4) {
     const float4 xr = reinterpret_cast<const float4 *>(P.xr32)[sidx];
-    rec[0] = xr.x + eoff_a(o) * (float)P.g.h[0];
-    rec[1] = xr.y + eoff_b(o) * (float)P.g.h[1];
-    rec[2] = (DIM == 3) ? xr.z + eoff_e(DIM, o) * (float)P.g.h[2] : 0.f;
-    rec[3] = 0.f;
+    const float x = xr.x + eoff_a(o) * (float)P.g.h[0];
+    const float y = xr.y + eoff_b(o) * (float)P.g.h[1];
+    const float z = (DIM == 3) ? xr.z + eoff_e(DIM, o) * (float)P.g.h[2] : 0.f;
+    rec[0] = x; rec[1] = x; rec[2] = y; rec[3] = y; rec[4] = z; rec[5] = z; rec[6] = 0.f; rec[7] = 0.f;
   } else {
     rec[0] = P.xs64[(size_t)sidx * DIM + 0];
     rec[1] = P.xs64[(size_t)sidx * DIM + 1];
     rec[2] = (DIM == 3) ? P.xs64[(size_t)sidx * DIM + 2] : 0.0;
     rec[3] = 0.0;
   }
+  /* coefficients field-major (field f, j-th involved patch), each repeated edup() times */
+  constexpr int H = ehead<Real>(), D = edup<Real>();
+  const int NI = epopc(mask);
   int j = 0;
   for (int k = 0; k < NEN; k++) {
     if (!((mask >> k) & 1)) continue;
-    Real *dst = rec + 4 + j * FP;
     if (setup[k]) {
       const long long pos = P.coff[node[k]] + P.slot[node[k] * 8 + eslot(DIM, k, o)] + pp;
       const size_t src = (size_t)pos * P.F + P.f0;
       for (int f = 0; f < FP; f++) {
-        if constexpr (sizeof(Real) == 4) dst[f] = P.c32[src + f];
-        else dst[f] = P.c64[src + f];
+        Real c;
+        if constexpr (sizeof(Real) == 4) c = P.c32[src + f];
+        else c = P.c64[src + f];
+        for (int q = 0; q < D; q++) rec[H + (f * NI + j) * D + q] = c;
       }
     } else {
-      for (int f = 0; f < FP; f++) dst[f] = Real(0);
+      for (int f = 0; f < FP; f++)
+        for (int q = 0; q < D; q++) rec[H + (f * NI + j) * D + q] = Real(0);
     }
     j++;
   }
-  for (int q = 4 + j * FP; q < S; q++) rec[q] = Real(0);
+  for (int q = H + NI * FP * D; q < S; q++) rec[q] = Real(0);
 }
 
 /* Per-CTA description of a cell's evaluation block: neighbour counts, first sorted index, corner

@@ -11,10 +11,10 @@ extern "C" int lgb_eval32_launch_2d(const EvalParams *P, int fp, int ker, int st
 extern "C" int lgb_build_records_3d(const EvalParams *P, int force, int grid, void *stream);
 extern "C" int lgb_build_records_2d(const EvalParams *P, int force, int grid, void *stream);
 
-/* Staging budgets (elements): FP32 gather 30 KB, FP32 TMA 2 x 12 KB (each + the running sums:
-   four to five CTAs per SM; measured best among 4/6/8/12/14/16 KB rings), FP64 48 KB. */
+/* Staging budgets (elements): FP32 gather 30 KB, FP32 TMA 2 x 8 KB (with the running sums: six
+   CTAs per SM; measured best among 4/6/8/12/16 KB rings with the packed FP32 loop), FP64 48 KB. */
 #define BUDGET32 7680
-#define BUDGET32_TMA 3072
+#define BUDGET32_TMA 2048
 #define BUDGET64 6144
 
 template <int DIM, int FP>

@@ -583,7 +583,7 @@ static int ensure_records(lgb_ctx *c)
       if (ni < 0 || ni >= g->nc[0] || nj < 0 || nj >= g->nc[1] || nl < 0 || nl >= g->nc[2]) continue;
       nb = ni + nj * g->nc[0] + nl * cxy;
       ninv = (a == 0 ? 2 : 1) * (b == 0 ? 2 : 1) * ((g->dim == 3 && e == 0) ? 2 : 1);
-      S = ((4 + ninv * g->dim + 3) / 4) * 4;
+      S = LGB_REC32_LEN(ninv, g->dim);
       total += (long long)(cs[nb + 1] - cs[nb]) * S;
     }
   }

@@ -36,6 +36,17 @@ enum { LGB_PREC_FP64 = 0, LGB_PREC_FP32 = 1 };
    (d->chunk_cap, a multiple of 64) is chosen from the particles-per-cell histogram. */
 #define LGB_CHUNK_MAX 256
 
+/* FP32 record of one data point in a cell's precomputed record block: a header {x, x, y, y, z, z,
+   0, 0} (coordinates relative to the evaluating cell's origin, each twice so that one 64-bit pair
+   holds a coordinate for two particles), then the coefficients of the ninv corner patches that
+   contain the point, field-major (field f, patch j at f*ninv + j), each stored LGB_REC32_DUP times,
+   padded to a multiple of 16 bytes. */
+#define LGB_REC32_HEAD 8
+#ifndef LGB_REC32_DUP
+#define LGB_REC32_DUP 1
+#endif
+#define LGB_REC32_LEN(ninv, fp) (((LGB_REC32_HEAD + (ninv) * (fp) * LGB_REC32_DUP + 3) / 4) * 4)
+
 /* PU mesh geometry (DMDA with Q1 elements): nodes are patches, elements are cells. */
 typedef struct {
   int dim, nen, kernel;
