@@ -397,3 +397,56 @@ extern "C" int lgb_op_mark_patches(lgb_dev *d, void *stream)
   LGB_CHECK_LAUNCH();
   return 0;
 }
+
+/* ------------------------------------------------------------------------------------------- */
+/* output assembly by pid straight into the caller's host arrays                                */
+/* ------------------------------------------------------------------------------------------- */
+/* AssembleArray_Allreduce (src/interface/interface_utils.c:188-263) on one rank: row pid - 1 of
+   each output holds the particle with that pid, rows of pids no longer in the swarm are zero.
+   The rows are written by the GPU directly into host memory (devices that access pageable memory
+   through the host's page tables, e.g. over NVLink-C2C), one pass, row-contiguous. */
+__global__ void k_pid_inverse(int n, const long long *__restrict__ pid, const int *__restrict__ alive, int nglobal,
+                              int *__restrict__ inv, int *__restrict__ bad)
+{
+  int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  if (alive && !alive[p]) return;
+  long long gi = pid[p] - 1;
+  if (gi < 0 || gi >= nglobal) {
+    atomicExch(bad, 1);
+    return;
+  }
+  inv[gi] = p;
+}
+
+__global__ void k_output_rows(int nglobal, const int *__restrict__ inv, int dim, const double *__restrict__ x,
+                              double *coords, int nf, const double *__restrict__ src, double *fields,
+                              const long long *__restrict__ pid, long long *pidx)
+{
+  for (long long gi = blockIdx.x * (long long)blockDim.x + threadIdx.x; gi < nglobal;
+       gi += (long long)gridDim.x * blockDim.x) {
+    const int p = inv[gi];
+    if (coords)
+      for (int d = 0; d < dim; d++) coords[gi * dim + d] = (p >= 0) ? x[(size_t)p * dim + d] : 0.0;
+    if (fields)
+      for (int f = 0; f < nf; f++) fields[gi * nf + f] = (p >= 0) ? src[(size_t)p * nf + f] : 0.0;
+    if (pidx) pidx[gi] = (p >= 0) ? pid[p] : 0;
+  }
+}
+
+extern "C" int lgb_op_output_rows(int n, const long long *pid, const int *alive, int nglobal, int *inv, int *bad,
+                                  int dim, const double *x, double *coords, int nf, const double *src, double *fields,
+                                  long long *pidx, int nsm, void *stream)
+{
+  cudaStream_t s = (cudaStream_t)stream;
+  cudaMemsetAsync(inv, 0xff, sizeof(int) * (size_t)(nglobal > 0 ? nglobal : 1), s); /* -1: no particle */
+  cudaMemsetAsync(bad, 0, sizeof(int), s);
+  if (n > 0) k_pid_inverse<<<lgb_cdiv(n, 256), 256, 0, s>>>(n, pid, alive, nglobal, inv, bad);
+  if (nglobal > 0) {
+    int grid = lgb_cdiv(nglobal, 256);
+    if (grid > 8 * nsm) grid = 8 * nsm;
+    k_output_rows<<<grid, 256, 0, s>>>(nglobal, inv, dim, x, coords, nf, src, fields, pid, pidx);
+  }
+  lgb_count_launch(2);
+  return (int)cudaGetLastError();
+}

@@ -35,28 +35,143 @@ struct FactorParams {
   lgb_ctrl *ctrl;
 };
 
-__device__ __forceinline__ double block_sum(double v, double *red)
+/* Column j of the lower factor from its diagonal element down: packed column-major (m(m+1)/2,
+   the kept factors) or the full column-major workspace.  L(i, j) = lcol(j)[i - j], i >= j. */
+template <bool PACKED>
+__device__ __forceinline__ const double *lcol(const double *L, int m, int j)
 {
-  for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
-  int w = threadIdx.x >> 5, l = threadIdx.x & 31;
-  __syncthreads();
-  if (l == 0) red[w] = v;
-  __syncthreads();
-  double s = 0.0;
-  if (threadIdx.x < 32) {
-    s = (threadIdx.x < FACT_T / 32) ? red[threadIdx.x] : 0.0;
-    for (int off = 16; off > 0; off >>= 1) s += __shfl_down_sync(0xffffffffu, s, off);
+  return PACKED ? L + ((long long)j * m - ((long long)j * (j - 1)) / 2) : L + (size_t)j * m + j;
+}
+
+/* Solves L L^T X = B in place for the F columns of B (B[f*m + i]), in blocks of 32 rows and four
+   right-hand sides at a time: the 32 x 32 diagonal block is staged in shared memory (D, 32 x 33)
+   and solved by one warp with shuffles, the block's solution is kept in shared memory (Y, 4 x 32),
+   and the rest of the patch is updated by all threads, each factor element read once per block
+   for all four right-hand sides.  The forward sweep subtracts L(i, j) y_j in ascending j for every
+   row, as a column sweep does. */
+template <bool PACKED>
+__device__ __forceinline__ long long lbase(int m, int j)
+{
+  return PACKED ? (long long)j * m - ((long long)j * (j - 1)) / 2 : (long long)j * m + j;
+}
+template <bool PACKED>
+__device__ __forceinline__ long long lstep(int m, int j)
+{
+  return PACKED ? (long long)(m - j) : (long long)m + 1; /* base(j + 1) - base(j) */
+}
+
+template <bool PACKED>
+__device__ void chol_solve_blocked(const double *L, int m, int F, double *B, double *D, double *Y)
+{
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarp = blockDim.x >> 5;
+  const int nblk = (m + 31) / 32;
+  for (int f0 = 0; f0 < F; f0 += 4) {
+    const int fc = min(4, F - f0);
+    double *B0 = B + (size_t)f0 * m;
+    /* forward: L y = b */
+    for (int kb = 0; kb < nblk; kb++) {
+      const int j0 = kb * 32, nb = min(32, m - j0);
+      for (int t = tid; t < nb * nb; t += blockDim.x) {
+        const int r = t / nb, c = t - r * nb;
+        if (r >= c) D[r * 33 + c] = L[lbase<PACKED>(m, j0 + c) + (r - c)];
+      }
+      __syncthreads();
+      if (warp == 0) {
+        double v[4];
+#pragma unroll
+        for (int q = 0; q < 4; q++) v[q] = (q < fc && lane < nb) ? B0[(size_t)q * m + j0 + lane] : 0.0;
+        for (int jj = 0; jj < nb; jj++) {
+          const double d = D[jj * 33 + jj];
+          const double l = (lane > jj && lane < nb) ? D[lane * 33 + jj] : 0.0;
+#pragma unroll
+          for (int q = 0; q < 4; q++) {
+            const double y = __shfl_sync(0xffffffffu, v[q], jj) / d;
+            if (lane == jj) v[q] = y;
+            else if (lane > jj) v[q] -= l * y;
+          }
+        }
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+          Y[q * 32 + lane] = v[q];
+          if (q < fc && lane < nb) B0[(size_t)q * m + j0 + lane] = v[q];
+        }
+      }
+      __syncthreads();
+      const long long b0 = lbase<PACKED>(m, j0);
+      for (int i = j0 + nb + tid; i < m; i += blockDim.x) {
+        double acc[4];
+#pragma unroll
+        for (int q = 0; q < 4; q++) acc[q] = (q < fc) ? B0[(size_t)q * m + i] : 0.0;
+        long long cb = b0 - j0; /* element (i, j) of column j at cb + i */
+#pragma unroll 8
+        for (int jj = 0; jj < nb; jj++) {
+          const double l = L[cb + i - jj];
+#pragma unroll
+          for (int q = 0; q < 4; q++)
+            if (q < fc) acc[q] -= l * Y[q * 32 + jj];
+          cb += lstep<PACKED>(m, j0 + jj);
+        }
+#pragma unroll
+        for (int q = 0; q < 4; q++)
+          if (q < fc) B0[(size_t)q * m + i] = acc[q];
+      }
+      __syncthreads();
+    }
+    /* backward: L^T x = y, blocks from the bottom */
+    for (int kb = nblk - 1; kb >= 0; kb--) {
+      const int i0 = kb * 32, nb = min(32, m - i0), k1 = i0 + nb;
+      /* y_i -= sum_{k >= k1} L(k, i) x_k for the block's rows: one warp per row */
+      for (int r = warp; r < nb; r += nwarp) {
+        const int i = i0 + r;
+        const double *ci = L + lbase<PACKED>(m, i) - i; /* L(k, i) = ci[k] */
+        double part[4] = {0.0, 0.0, 0.0, 0.0};
+#pragma unroll 4
+        for (int k = k1 + lane; k < m; k += 32) {
+          const double l = ci[k];
+#pragma unroll
+          for (int q = 0; q < 4; q++)
+            if (q < fc) part[q] += l * B0[(size_t)q * m + k];
+        }
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+          double pq = part[q];
+          for (int off = 16; off > 0; off >>= 1) pq += __shfl_down_sync(0xffffffffu, pq, off);
+          if (lane == 0 && q < fc) B0[(size_t)q * m + i] -= pq;
+        }
+      }
+      for (int t = tid; t < nb * nb; t += blockDim.x) {
+        const int r = t / nb, c = t - r * nb;
+        if (r >= c) D[r * 33 + c] = L[lbase<PACKED>(m, i0 + c) + (r - c)];
+      }
+      __syncthreads();
+      if (warp == 0) {
+        double v[4];
+#pragma unroll
+        for (int q = 0; q < 4; q++) v[q] = (q < fc && lane < nb) ? B0[(size_t)q * m + i0 + lane] : 0.0;
+        for (int ii = nb - 1; ii >= 0; ii--) {
+          const double d = D[ii * 33 + ii];
+          const double l = (lane < ii) ? D[ii * 33 + lane] : 0.0;
+#pragma unroll
+          for (int q = 0; q < 4; q++) {
+            const double x = __shfl_sync(0xffffffffu, v[q], ii) / d;
+            if (lane == ii) v[q] = x;
+            else if (lane < ii) v[q] -= l * x;
+          }
+        }
+#pragma unroll
+        for (int q = 0; q < 4; q++)
+          if (q < fc && lane < nb) B0[(size_t)q * m + i0 + lane] = v[q];
+      }
+      __syncthreads();
+    }
   }
-  if (threadIdx.x == 0) red[FACT_T / 32] = s;
-  __syncthreads();
-  return red[FACT_T / 32];
 }
 
 __global__ void __launch_bounds__(FACT_T) k_factor(FactorParams P)
 {
   __shared__ int s_cstart[8], s_cnt[8], s_off[8];
-  __shared__ double red[FACT_T / 32 + 1];
   __shared__ int s_fail;
+  __shared__ double s_diag[32 * 33], s_y[4 * 32];
   const lgb_geom &g = P.g;
   const int nwork = P.ctrl->nwork;
   const int tid = threadIdx.x;
@@ -146,38 +261,12 @@ __global__ void __launch_bounds__(FACT_T) k_factor(FactorParams P)
         atomicAdd(&P.ctrl->nfactored, 1);
       }
     } else if (m > 0) {
-      const double *Fk = P.fac + P.foff[node];
-      for (int j = 0; j < m; j++) {
-        long long base = (long long)j * m - ((long long)j * (j - 1)) / 2;
-        for (int i = j + tid; i < m; i += FACT_T) A[(size_t)j * m + i] = Fk[base + (i - j)];
-      }
       if (tid == 0) atomicAdd(&P.ctrl->factor_flops, 2.0 * (double)m * m * F);
     }
     __syncthreads();
     if (m > 0) {
-      /* forward: L y = b (column sweep, coalesced column reads) */
-      for (int j = 0; j < m; j++) {
-        const double ljj = A[(size_t)j * m + j];
-        for (int f = 0; f < F; f++) {
-          double yj = B[(size_t)f * m + j] / ljj;
-          for (int i = j + 1 + tid; i < m; i += FACT_T) B[(size_t)f * m + i] -= A[(size_t)j * m + i] * yj;
-        }
-        __syncthreads();
-        if (tid == 0)
-          for (int f = 0; f < F; f++) B[(size_t)f * m + j] /= ljj;
-        __syncthreads();
-      }
-      /* backward: L^T x = y (dot products with column i) */
-      for (int i = m - 1; i >= 0; i--) {
-        const double lii = A[(size_t)i * m + i];
-        for (int f = 0; f < F; f++) {
-          double part = 0.0;
-          for (int k = i + 1 + tid; k < m; k += FACT_T) part += A[(size_t)i * m + k] * B[(size_t)f * m + k];
-          double sum = block_sum(part, red);
-          if (tid == 0) B[(size_t)f * m + i] = (B[(size_t)f * m + i] - sum) / lii;
-          __syncthreads();
-        }
-      }
+      if (have_factor) chol_solve_blocked<true>(P.fac + P.foff[node], m, F, B, s_diag, s_y);
+      else chol_solve_blocked<false>(A, m, F, B, s_diag, s_y);
       /* coefficients [point][field] in both precisions */
       const long long c0 = P.coff[node];
       for (int q = tid; q < m; q += FACT_T)

@@ -220,6 +220,12 @@ typedef struct {
   /* host mirrors */
   int64_t *pid_d, *pid_p;
   int pid_d_cap, pid_p_cap;
+  /* direct output: device copy of the particle pids, pid -> swarm index scratch, status flag */
+  int out_direct;        /* option output_direct and the device reads/writes pageable host memory */
+  long long *pidd;
+  int pidd_cap, pidd_valid;
+  int *out_inv, *out_bad;
+  long long out_inv_cap;
   double *hx_d;          /* last filled data coordinates (change detection) */
   int data_filled, points_filled;
   vfn_t vfn;
@@ -287,6 +293,7 @@ static void destroy_ctx(lgb_ctx *c)
   for (i = 0; i < 2 * NPROF; i++) if (c->ev[i]) cudaEventDestroy(c->ev[i]);
   if (c->hctrl) cudaFreeHost(c->hctrl);
   if (c->stream) cudaStreamDestroy(c->stream);
+  DFREE(c->pidd); DFREE(c->out_inv); DFREE(c->out_bad);
   free(c->pid_d); free(c->pid_p); free(c->hx_d);
   free(c);
 }
@@ -381,6 +388,8 @@ static int read_options(lgb_ctx *c)
   }
   c->use_graph = 1;
   opt_bool("use_cuda_graph", &c->use_graph);
+  c->out_direct = 1;
+  opt_bool("output_direct", &c->out_direct);
   return 0;
 }
 
@@ -400,6 +409,14 @@ static int create_ctx(lgb_ctx **out)
     }
   }
   if (lgb_device_info(&d->nsm, &d->smem_optin)) { free(c); return set_error(LAGRBF_ERR_GPU, "no CUDA device"); }
+  {
+    /* direct output needs coherent device access to pageable host memory (host page tables) */
+    int dev = 0, pageable = 0, host_pt = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, dev);
+    cudaDeviceGetAttribute(&host_pt, cudaDevAttrPageableMemoryAccessUsesHostPageTables, dev);
+    c->out_direct = c->out_direct && pageable && host_pt;
+  }
   if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
     free(c);
     return set_error(LAGRBF_ERR_GPU, "cudaStreamCreate failed");
@@ -536,12 +553,12 @@ static int ensure_pools(lgb_ctx *c)
       if (err) { d->fac_cap = 0; return set_error(LAGRBF_ERR_MEM, "factor pool allocation failed (%lld doubles)", ftotal); }
     }
   }
-  /* factorisation workspace: per slot m^2 + m*(dim+F) doubles, up to 2 slots per SM within ~4 GB */
+  /* factorisation workspace: per slot m^2 + m*(dim+F) doubles, up to 4 slots per SM within ~4 GB */
   {
     long long m = d->max_patch > 0 ? d->max_patch : 1;
     long long stride = m * m + m * (d->g.dim + d->F) + 32;
     long long budget = 4LL << 30;
-    int nws = 2 * d->nsm;
+    int nws = 4 * d->nsm; /* four patches per SM in flight: the solves are latency bound */
     if ((long long)nws * stride * 8 > budget) nws = (int)(budget / (stride * 8));
     if (nws < 1) nws = 1;
     if (stride != d->ws_stride || nws != d->nws) {
@@ -704,6 +721,7 @@ static int fill_points(lgb_ctx *c, int n, const double *coords, const double *va
   TRY(grow_pids(&c->pid_p, &c->pid_p_cap, old, n));
   if (pidx) memcpy(c->pid_p, pidx, sizeof(int64_t) * (size_t)n);
   else assign_pids(c->pid_p, old, n);
+  c->pidd_valid = 0;
   if (n > d->np_cap) {
     /* keep the old field contents of the first `old` particles (the swarm keeps them) */
     double *of = d->fields, *ov = d->vel;
@@ -1059,6 +1077,36 @@ static int do_output(lgb_ctx *c, int is_data, int nglobal, double *coords, doubl
       OP(lgb_op_weights(d, wtmp, c->stream));
       src = wtmp;
     } else return set_error(LAGRBF_ERR_ARG_WRONG, "unknown field \"%s\"", fieldname);
+  }
+  if (!is_data && c->out_direct) {
+    /* the GPU writes every output row into the caller's arrays (pid order, zero rows for pids no
+       longer in the swarm) */
+    int err = 0, bad = 0;
+    if (n > c->pidd_cap) {
+      DFREE(c->pidd);
+      c->pidd = (long long *)dalloc(sizeof(long long) * (size_t)n, &err);
+      c->pidd_cap = err ? 0 : n;
+      c->pidd_valid = 0;
+    }
+    if (!c->pidd_valid && n > 0 && !err) {
+      CU(cudaMemcpyAsync(c->pidd, c->pid_p, sizeof(long long) * (size_t)n, cudaMemcpyHostToDevice, c->stream));
+      c->pidd_valid = 1;
+    }
+    if (!err && (long long)nglobal > c->out_inv_cap) {
+      DFREE(c->out_inv);
+      c->out_inv = (int *)dalloc(sizeof(int) * (size_t)(nglobal > 0 ? nglobal : 1), &err);
+      c->out_inv_cap = err ? 0 : nglobal;
+    }
+    if (!err && !c->out_bad) c->out_bad = (int *)dalloc(sizeof(int), &err);
+    if (err) { rc = set_error(LAGRBF_ERR_MEM, "output scratch allocation failed"); goto done; }
+    OP(lgb_op_output_rows(n, c->pidd, d->alive, nglobal, c->out_inv, c->out_bad, dim, d->xp, coords, nf, src, fields,
+                          (long long *)pidx, d->nsm, c->stream));
+    CU(cudaMemcpyAsync(&c->hctrl->eval_error, c->out_bad, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    CU(cudaStreamSynchronize(c->stream));
+    bad = c->hctrl->eval_error;
+    c->hctrl->eval_error = 0;
+    if (bad) rc = set_error(LAGRBF_ERR_ARG_OUTOFRANGE, "a particle pid is out of range [1, %d]", nglobal);
+    goto done;
   }
   hx = (double *)malloc(sizeof(double) * (size_t)(n > 0 ? n : 1) * dim);
   hf = (double *)malloc(sizeof(double) * (size_t)(n > 0 ? n : 1) * (nf > 0 ? nf : 1));

