@@ -125,6 +125,16 @@ typedef struct {
 /* The interpolated advection loop of lagrbf_advect_interpolate over [time, time_next] without its
    end-of-call reset: the data swarm, binning and patch set-ups stay resident for the next call. */
 LAGRBF_EXPORT int lagrbf_gpu_advect_resident(void *ctx, double time, double time_next);
+/* Device-side analytical velocity for lagrbf_avect_analytical (replaces the per-stage host
+   callback round trip of lagrbf_advection_function(_batch); takes precedence over a registered
+   callback; kind 0 removes it).  Parameters:
+     LAGRBF_VFIELD_ROTATION {omega, cx, cy}:  v = omega (-(y - cy), x - cx, 0)
+     LAGRBF_VFIELD_CELLULAR {a, k}:           v = a (sin(k pi x) cos(k pi y), -cos(k pi x) sin(k pi y), 0)
+     LAGRBF_VFIELD_ABC      {A, B, C, s}:     X = s x: (A sin Z + C cos Y, B sin X + A cos Z, C sin Y + B cos X)
+     LAGRBF_VFIELD_FOURIER  {n, n x (k1, k2, k3, phase, a1, a2, a3)}: v_c = sum_m a_mc sin(2 pi k_m.x + phase_m) */
+enum { LAGRBF_VFIELD_NONE = 0, LAGRBF_VFIELD_ROTATION = 1, LAGRBF_VFIELD_CELLULAR = 2, LAGRBF_VFIELD_ABC = 3,
+       LAGRBF_VFIELD_FOURIER = 4 };
+LAGRBF_EXPORT int lagrbf_gpu_set_velocity_field(void *ctx, int32_t kind, const double *params, int32_t nparams);
 /* Switches the evaluation precision of a live context (1: FP32 evaluation, 0: FP64). */
 LAGRBF_EXPORT int lagrbf_gpu_set_precision(void *ctx, int fp32);
 /* FP32 FMA throughput of the current device in TFLOP/s, measured by a synthetic kernel

@@ -233,6 +233,16 @@ class LagRBFCtx:
         self._check(self._cf["lagrbf_gpu_advect_resident"](self.ctx, float(time_start), float(time_end)),
                     "lagrbf_gpu_advect_resident")
 
+    VFIELD_NONE, VFIELD_ROTATION, VFIELD_CELLULAR, VFIELD_ABC, VFIELD_FOURIER = 0, 1, 2, 3, 4
+
+    def set_velocity_field(self, kind, params=None):
+        """Device-side analytical velocity for advect_analytical_c (lagrbf_gpu_set_velocity_field):
+        ROTATION (omega, cx, cy), CELLULAR (a, k), ABC (A, B, C, scale), FOURIER (n, then n rows of
+        k1, k2, k3, phase, a1, a2, a3); kind 0 removes it."""
+        p = None if params is None else np.ascontiguousarray(np.ravel(params), dtype=np.float64)
+        n = 0 if p is None else int(p.size)
+        self._check(self._cf["lagrbf_gpu_set_velocity_field"](self.ctx, int(kind), p, n), "lagrbf_gpu_set_velocity_field")
+
     def set_precision(self, fp32):
         self._check(self._cf["lagrbf_gpu_set_precision"](self.ctx, int(bool(fp32))), "lagrbf_gpu_set_precision")
 

@@ -233,7 +233,7 @@ typedef struct {
   void *vuser;
   /* graph of one internal step */
   cudaGraphExec_t graph;
-  int graph_valid;
+  int graph_valid, graph_mode; /* graph_mode: 1 when the captured step is analytical */
   long long graph_launches, graph_eval_launches;
   /* pinned control copy */
   lgb_ctrl *hctrl;
@@ -293,7 +293,7 @@ static void destroy_ctx(lgb_ctx *c)
   for (i = 0; i < 2 * NPROF; i++) if (c->ev[i]) cudaEventDestroy(c->ev[i]);
   if (c->hctrl) cudaFreeHost(c->hctrl);
   if (c->stream) cudaStreamDestroy(c->stream);
-  DFREE(c->pidd); DFREE(c->out_inv); DFREE(c->out_bad);
+  DFREE(c->pidd); DFREE(c->out_inv); DFREE(c->out_bad); DFREE(d->vfield_par);
   free(c->pid_d); free(c->pid_p); free(c->hx_d);
   free(c);
 }
@@ -927,7 +927,9 @@ static int step_sequence(lgb_ctx *c, int analytical)
 
 static int run_step(lgb_ctx *c, int analytical)
 {
-  if (analytical || c->profiling || !c->use_graph) {
+  /* the captured step differs between interpolated and device-field analytical advection */
+  if (c->graph_valid && c->graph_mode != analytical) invalidate_graph(c);
+  if ((analytical && !c->d.vfield) || c->profiling || !c->use_graph) {
     long long l0 = lgb_launch_count();
     TRY(step_sequence(c, analytical));
     c->launches_graph += 0;
@@ -943,7 +945,7 @@ static int run_step(lgb_ctx *c, int analytical)
     cudaError_t e = cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal);
     int rc = 0;
     if (e == cudaSuccess) {
-      rc = step_sequence(c, 0);
+      rc = step_sequence(c, analytical);
       e = cudaStreamEndCapture(c->stream, &graph);
     }
     c->graph_eval_launches = c->eval_launches - e0;
@@ -952,16 +954,17 @@ static int run_step(lgb_ctx *c, int analytical)
       /* capture not possible: run this step eagerly and stop using graphs */
       cudaGetLastError();
       c->use_graph = 0;
-      TRY(step_sequence(c, 0));
+      TRY(step_sequence(c, analytical));
     } else {
       e = cudaGraphInstantiate(&c->graph, graph, 0);
       cudaGraphDestroy(graph);
       if (e != cudaSuccess) {
         cudaGetLastError();
         c->use_graph = 0;
-        TRY(step_sequence(c, 0));
+        TRY(step_sequence(c, analytical));
       } else {
         c->graph_valid = 1;
+        c->graph_mode = analytical;
         c->graph_launches = lgb_launch_count() - l0;
         /* the captured launches did not run; count them when the graph replays */
         c->launch_base += c->graph_launches;
@@ -1018,12 +1021,17 @@ static int advection_loop(lgb_ctx *c, double t, double t_next, int analytical, i
 static int host_velocity(lgb_ctx *c)
 {
   /* AdvectionEvaluateVelocityFunction (advection.c:318-351): the callback sees the live
-     particles packed contiguously, like the swarm after migration. */
+     particles packed contiguously, like the swarm after migration.  A device-side field, when set,
+     replaces the callback and stays on the stream. */
   lgb_dev *d = &c->d;
   int dim = d->g.dim, n = d->np, p, q = 0, nl = 0, rc = 0;
   double *x = NULL, *v = NULL, *xc = NULL, *vc = NULL;
   int *alive = NULL;
   if (n == 0) return 0;
+  if (d->vfield) {
+    OP(lgb_op_velocity_field(d, c->stream));
+    return 0;
+  }
   x = (double *)malloc(sizeof(double) * (size_t)n * dim);
   v = (double *)malloc(sizeof(double) * (size_t)n * dim);
   xc = (double *)malloc(sizeof(double) * (size_t)n * dim);
@@ -1188,7 +1196,7 @@ LAGRBF_EXPORT int lagrbf_avect_analytical(void *ctx, double time, double time_ne
 {
   lgb_ctx *c = (lgb_ctx *)ctx;
   if (!c) return set_error(LAGRBF_ERR_ARG_NULL, "LagRBFCtx is NULL");
-  if (!c->vfn && !c->vfnb) return set_error(LAGRBF_ERR_ARG_NULL, "no velocity function registered");
+  if (!c->vfn && !c->vfnb && !c->d.vfield) return set_error(LAGRBF_ERR_ARG_NULL, "no velocity function registered");
   return advection_loop(c, time, time_next, 1, 0);
 }
 
@@ -1249,6 +1257,42 @@ LAGRBF_EXPORT int lagrbf_gpu_advect_resident(void *ctx, double time, double time
 
 double lgb_fp32_peak_tflops(void);
 LAGRBF_EXPORT double lagrbf_gpu_fp32_peak_tflops(void) { return lgb_fp32_peak_tflops(); }
+
+LAGRBF_EXPORT int lagrbf_gpu_set_velocity_field(void *ctx, int32_t kind, const double *params, int32_t nparams)
+{
+  lgb_ctx *c = (lgb_ctx *)ctx;
+  lgb_dev *d;
+  int need = 0, err = 0;
+  if (!c) return set_error(LAGRBF_ERR_ARG_NULL, "context is NULL");
+  d = &c->d;
+  switch (kind) {
+  case LGB_VF_NONE: need = 0; break;
+  case LGB_VF_ROTATION: need = 3; break;
+  case LGB_VF_CELLULAR: need = 2; break;
+  case LGB_VF_ABC: need = 4; break;
+  case LGB_VF_FOURIER:
+    if (nparams < 1 || !params) return set_error(LAGRBF_ERR_ARG_SIZ, "Fourier field: parameters missing");
+    if (!(params[0] >= 0.0) || params[0] > 4096.0) return set_error(LAGRBF_ERR_ARG_OUTOFRANGE, "Fourier field: bad mode count");
+    need = 1 + 7 * (int)params[0];
+    break;
+  default: return set_error(LAGRBF_ERR_ARG_OUTOFRANGE, "unknown velocity field kind %d", kind);
+  }
+  if (nparams < need || (need > 0 && !params))
+    return set_error(LAGRBF_ERR_ARG_SIZ, "velocity field kind %d needs %d parameters, got %d", kind, need, nparams);
+  CU(cudaStreamSynchronize(c->stream));
+  DFREE(d->vfield_par);
+  d->vfield = 0;
+  d->vfield_np = 0;
+  if (kind != LGB_VF_NONE) {
+    d->vfield_par = (double *)dalloc(sizeof(double) * (size_t)(need > 0 ? need : 1), &err);
+    if (err) return set_error(LAGRBF_ERR_MEM, "velocity field parameters allocation failed");
+    if (need > 0) CU(cudaMemcpy(d->vfield_par, params, sizeof(double) * (size_t)need, cudaMemcpyHostToDevice));
+    d->vfield = kind;
+    d->vfield_np = need;
+  }
+  invalidate_graph(c);
+  return 0;
+}
 
 LAGRBF_EXPORT int lagrbf_gpu_set_precision(void *ctx, int fp32)
 {

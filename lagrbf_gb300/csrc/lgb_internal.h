@@ -31,6 +31,8 @@ enum { LGB_KERNEL_LINEAR = 0, LGB_KERNEL_WENDLAND_C0, LGB_KERNEL_WENDLAND_C2, LG
 enum { LGB_RK1 = 0, LGB_RK2 = 1, LGB_RK4 = 2, LGB_DOPRI = 3 };
 enum { LGB_A_FACTOR = 0, LGB_A_KSP = 1, LGB_A_KSP_ASMB = 2 };
 enum { LGB_PREC_FP64 = 0, LGB_PREC_FP32 = 1 };
+/* Device-side analytical velocity fields (LAGRBF_VFIELD_* of the public header). */
+enum { LGB_VF_NONE = 0, LGB_VF_ROTATION = 1, LGB_VF_CELLULAR = 2, LGB_VF_ABC = 3, LGB_VF_FOURIER = 4 };
 
 /* Largest evaluation work unit (particles of one cell handled by one CTA); the actual capacity
    (d->chunk_cap, a multiple of 64) is chosen from the particles-per-cell histogram. */
@@ -122,6 +124,9 @@ typedef struct {
   /* scratch for scans */
   int *scan_tmp;
   long long *scan_tmp64;
+  /* device-side analytical velocity: kind, parameters (device) and their count */
+  int vfield, vfield_np;
+  double *vfield_par;
   /* control */
   lgb_ctrl *ctrl;
   int smem_optin;      /* cudaDevAttrMaxSharedMemoryPerBlockOptin */
@@ -152,6 +157,7 @@ int lgb_op_ctrl(lgb_dev *d, int what, void *stream);
 enum { LGB_CTRL_BEGIN_STEP = 0, LGB_CTRL_END_STEP = 1, LGB_CTRL_RESET_CFL = 2, LGB_CTRL_DOPRI_DT = 3 };
 int lgb_op_copy_velocity(lgb_dev *d, void *stream);     /* vel <- fields[:, :dim] */
 int lgb_op_count_alive(lgb_dev *d, void *stream);
+int lgb_op_velocity_field(lgb_dev *d, void *stream);    /* vel <- analytical field at live particles */
 int lgb_device_info(int *nsm, int *smem_optin);
 /* Output rows by pid (inv: nglobal ints of scratch, bad: one int, set when a pid is out of range);
    coords / fields / pidx may be host pointers the device can access. */

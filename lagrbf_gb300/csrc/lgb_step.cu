@@ -13,6 +13,7 @@
  * doubles.  The loop scalars (t, dt, DOPRI dt) live in a device control block, so a whole
  * internal step is a fixed sequence of launches that the host captures once in a CUDA graph.
  */
+#include <math.h>
 #include "lgb_common.cuh"
 #include <float.h>
 
@@ -209,6 +210,66 @@ extern "C" int lgb_op_count_alive(lgb_dev *d, void *stream)
   if (d->np <= 0) return 0;
   k_velocity_cfl<<<lgb_cdiv(d->np, 256), 256, 0, (cudaStream_t)stream>>>(d->np, d->g.dim, d->F, 0, d->fields,
                                                                            d->vel, d->alive, d->ctrl);
+  lgb_count_launch(1);
+  return (int)cudaGetLastError();
+}
+
+/* Analytical velocity evaluated on the device at the live particles, in place of the host
+   callback of AdvectionEvaluateVelocityFunction (advection.c:318-351), so that analytical advection
+   needs no host round trip per stage.  Fields (par = parameters):
+     ROTATION  par {omega, cx, cy}: v = omega (-(y - cy), x - cx, 0)
+     CELLULAR  par {a, k}:          v = a (sin(k pi x) cos(k pi y), -cos(k pi x) sin(k pi y), 0)
+     ABC       par {A, B, C, s}:    X = s x: v = (A sin Z + C cos Y, B sin X + A cos Z, C sin Y + B cos X)
+     FOURIER   par {n, then n x (k1, k2, k3, phase, a1, a2, a3)}:
+                                    v_c = sum_m a_mc sin(2 pi (k_m . x) + phase_m)
+   Velocities of removed particles are left as they are, like the host path. */
+__global__ void k_velocity_field(int np, int dim, const double *__restrict__ x, const int *__restrict__ alive,
+                                 double *__restrict__ v, int kind, const double *__restrict__ par, int npar)
+{
+  int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= np || !alive[p]) return;
+  const double *xp = x + (size_t)p * dim;
+  double X = xp[0], Y = xp[1], Z = (dim == 3) ? xp[2] : 0.0;
+  double o[3] = {0.0, 0.0, 0.0};
+  switch (kind) {
+  case LGB_VF_ROTATION:
+    o[0] = -par[0] * (Y - par[2]);
+    o[1] = par[0] * (X - par[1]);
+    break;
+  case LGB_VF_CELLULAR: {
+    const double kx = par[1] * M_PI * X, ky = par[1] * M_PI * Y;
+    o[0] = par[0] * sin(kx) * cos(ky);
+    o[1] = -par[0] * cos(kx) * sin(ky);
+    break;
+  }
+  case LGB_VF_ABC: {
+    const double a = par[3] * X, b = par[3] * Y, c = par[3] * Z;
+    o[0] = par[0] * sin(c) + par[2] * cos(b);
+    o[1] = par[1] * sin(a) + par[0] * cos(c);
+    o[2] = par[2] * sin(b) + par[1] * cos(a);
+    break;
+  }
+  case LGB_VF_FOURIER: {
+    const int nm = (int)par[0];
+    for (int m = 0; m < nm && 1 + 7 * m + 6 < npar; m++) {
+      const double *q = par + 1 + 7 * m;
+      const double s = sin(2.0 * M_PI * (q[0] * X + q[1] * Y + q[2] * Z) + q[3]);
+      o[0] += q[4] * s;
+      o[1] += q[5] * s;
+      o[2] += q[6] * s;
+    }
+    break;
+  }
+  default: break;
+  }
+  for (int d = 0; d < dim; d++) v[(size_t)p * dim + d] = o[d];
+}
+
+extern "C" int lgb_op_velocity_field(lgb_dev *d, void *stream)
+{
+  if (d->np <= 0 || !d->vfield) return 0;
+  k_velocity_field<<<lgb_cdiv(d->np, 256), 256, 0, (cudaStream_t)stream>>>(d->np, d->g.dim, d->xp, d->alive, d->vel,
+                                                                              d->vfield, d->vfield_par, d->vfield_np);
   lgb_count_launch(1);
   return (int)cudaGetLastError();
 }
