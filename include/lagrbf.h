@@ -160,6 +160,30 @@ LAGRBF_EXPORT int64_t lagrbf_gpu_get_block_csr(void *ctx, int32_t *blk_start, in
 /* Geometry of the context: dim, n[3], nnodes, ncells, nen and eps_w, eps_r. */
 LAGRBF_EXPORT int lagrbf_gpu_get_geometry(void *ctx, int32_t *ints /* 7 */, double *reals /* 2 */);
 
+/* ---------------------------------------------------------------------------------------- */
+/* 4. PETSc binary files (no PETSc needed)                                                   */
+/* ---------------------------------------------------------------------------------------- */
+/* PETSc binary viewer format, 32-bit PetscInt, big-endian: Vec = class id 1211214, n, n doubles;
+   IS = class id 1211218, n, n int32.  A Vec's block size is read from / written to "<path>.info"
+   ("-vecload_block_size <bs>").  Readers: pass NULL for the buffer to get the length first.
+   Replace VecLoadFromFile / ISLoadFromFile (src/io_utils.c:211-238) and the VecView / ISView
+   writers of src/swarm/swarm_output.c:87-166. */
+LAGRBF_EXPORT int lagrbf_petsc_vec_write(const char *path, const double *values, int64_t n, int32_t block_size);
+LAGRBF_EXPORT int lagrbf_petsc_vec_read(const char *path, double *values, int64_t capacity, int64_t *n,
+                                        int32_t *block_size);
+LAGRBF_EXPORT int lagrbf_petsc_is_write(const char *path, const int64_t *indices, int64_t n);
+LAGRBF_EXPORT int lagrbf_petsc_is_read(const char *path, int64_t *indices, int64_t capacity, int64_t *n);
+/* SwarmSetFromPetscFiles (src/readers/petsc_loader/petsc_loader.c:38-99): coordinates from
+   coords_file (block size dim) set the number of points; the field files fill
+   n_interpolation_fields in file order by block; pid_file (nullable, an IS) gives the pids
+   (SwarmInterpLoadPidxFromFile, src/swarm/swarm_interp.c:180-222).  Then lagrbf_fill_swarm. */
+LAGRBF_EXPORT int lagrbf_fill_swarm_from_files(void *ctx, bool is_data, const char *coords_file,
+                                               const char **field_files, int32_t nfiles, const char *pid_file);
+/* lagrbf_output into files: <prefix>_coor.pbvec, <prefix>_<fieldname>.pbvec (with .info) and
+   <prefix>_pid.pbis, nglobal rows assembled by pid. */
+LAGRBF_EXPORT int lagrbf_output_files(void *ctx, bool is_data, int32_t nglobal, const char *prefix,
+                                      const char *fieldname);
+
 /* Binning without device allocation (no counterpart in the reference).  For callers that may not
    have a library allocate device memory at this point: a code running its time loop from a device
    pool reserved at start-up, or one recording its step into its own stream capture.  Bins npoints

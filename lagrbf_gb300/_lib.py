@@ -95,6 +95,11 @@ def register_functions(clib):
     reg("lagrbf_gpu_advect_resident", ctypes.c_int, [ctypes.c_void_p, PetscReal, PetscReal])
     reg("lagrbf_gpu_set_precision", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int])
     reg("lagrbf_gpu_set_velocity_field", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, real_pn, ctypes.c_int32])
+    reg("lagrbf_fill_swarm_from_files", ctypes.c_int, [ctypes.c_void_p, ctypes.c_bool, ctypes.c_char_p,
+                                                       ctypes.POINTER(ctypes.c_char_p), ctypes.c_int32,
+                                                       ctypes.c_char_p])
+    reg("lagrbf_output_files", ctypes.c_int, [ctypes.c_void_p, ctypes.c_bool, ctypes.c_int32, ctypes.c_char_p,
+                                              ctypes.c_char_p])
     reg("lagrbf_gpu_fp32_peak_tflops", ctypes.c_double, [])
     reg("lagrbf_gpu_get_stats", ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Stats)])
     reg("lagrbf_gpu_reset_stats", ctypes.c_int, [ctypes.c_void_p])

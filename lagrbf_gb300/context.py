@@ -233,6 +233,25 @@ class LagRBFCtx:
         self._check(self._cf["lagrbf_gpu_advect_resident"](self.ctx, float(time_start), float(time_end)),
                     "lagrbf_gpu_advect_resident")
 
+    def fill_from_files(self, coords_file, field_files=(), pid_file=None, is_data=False):
+        """lagrbf_fill_swarm_from_files: a swarm from PETSc binary files (coordinates, fields stacked
+        in file order, optional pid index set)."""
+        arr = (ctypes.c_char_p * max(len(field_files), 1))(*[str(f).encode() for f in field_files])
+        rc = self._cf["lagrbf_fill_swarm_from_files"](self.ctx, bool(is_data), str(coords_file).encode(), arr,
+                                                      len(field_files),
+                                                      None if pid_file is None else str(pid_file).encode())
+        self._check(rc, "lagrbf_fill_swarm_from_files")
+        if is_data:
+            self.data_filled = True
+        else:
+            self.interp_filled = True
+
+    def output_files(self, prefix, npoints, fieldname="fields", is_data=False):
+        """lagrbf_output_files: <prefix>_coor.pbvec, <prefix>_<fieldname>.pbvec, <prefix>_pid.pbis."""
+        rc = self._cf["lagrbf_output_files"](self.ctx, bool(is_data), int(npoints), str(prefix).encode(),
+                                             fieldname.encode())
+        self._check(rc, "lagrbf_output_files")
+
     VFIELD_NONE, VFIELD_ROTATION, VFIELD_CELLULAR, VFIELD_ABC, VFIELD_FOURIER = 0, 1, 2, 3, 4
 
     def set_velocity_field(self, kind, params=None):

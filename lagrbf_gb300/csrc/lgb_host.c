@@ -50,6 +50,9 @@ LAGRBF_EXPORT const char *lagrbf_gpu_last_error(void) { return g_errmsg; }
 
 int lgb_set_error_msg(int code, const char *msg) { return set_error(code, "%s", msg); }
 
+/* Mesh dimension and number of interpolation fields of a context (file loaders). */
+int lgb_ctx_dims(void *ctx, int *dim, int *nfields);
+
 #define CU(call)                                                                                    \
   do {                                                                                              \
     cudaError_t e_ = (call);                                                                        \
@@ -1472,5 +1475,14 @@ LAGRBF_EXPORT int lagrbf_gpu_get_geometry(void *ctx, int32_t *ints, double *real
   ints[0] = c->d.g.dim; ints[1] = c->d.g.n[0]; ints[2] = c->d.g.n[1]; ints[3] = c->d.g.n[2];
   ints[4] = c->d.g.nnodes; ints[5] = c->d.g.ncells; ints[6] = c->d.g.nen;
   reals[0] = c->d.g.eps_w; reals[1] = c->d.g.eps_r;
+  return 0;
+}
+
+int lgb_ctx_dims(void *ctx, int *dim, int *nfields)
+{
+  lgb_ctx *c = (lgb_ctx *)ctx;
+  if (!c) return set_error(LAGRBF_ERR_ARG_NULL, "context is NULL");
+  *dim = c->d.g.dim;
+  *nfields = c->d.F;
   return 0;
 }

@@ -330,6 +330,37 @@ def test_device_velocity_field_validation():
     c.set_velocity_field(0)
 
 
+def test_fill_from_petsc_files_equals_arrays(tmp_path):
+    """lagrbf_fill_swarm_from_files (coordinates, two field files stacked by block, pid IS) gives
+    the same interpolation as filling from arrays, and lagrbf_output_files writes what
+    lagrbf_output returns."""
+    from lagrbf_gb300 import petsc_io as PIO
+    xd, fd, xp, opts = small_3d(np_=800)
+    pid = np.arange(1, len(xp) + 1, dtype=np.int64) * 2
+    PIO.write_vec(tmp_path / "dcoor.pbvec", xd)
+    PIO.write_vec(tmp_path / "f01.pbvec", fd[:, :2])
+    PIO.write_vec(tmp_path / "f2.pbvec", fd[:, 2])
+    PIO.write_vec(tmp_path / "pcoor.pbvec", xp)
+    PIO.write_is(tmp_path / "ppid.pbis", pid)
+    a = gpu_ctx(opts)
+    a.fill_data(xd, fd); a.fill_points(xp, pidx=pid); a.interpolate_c()
+    b = gpu_ctx(opts)
+    b.fill_from_files(tmp_path / "dcoor.pbvec", [tmp_path / "f01.pbvec", tmp_path / "f2.pbvec"], is_data=True)
+    b.fill_from_files(tmp_path / "pcoor.pbvec", pid_file=tmp_path / "ppid.pbis")
+    b.interpolate_c()
+    n = int(pid.max())
+    ra, rb = gpu_output(a, n, 3), gpu_output(b, n, 3)
+    for u, v in zip(ra, rb):
+        assert np.array_equal(u, v)
+    b.output_files(tmp_path / "out", n)
+    assert np.array_equal(PIO.read_vec(tmp_path / "out_coor.pbvec"), rb[0])
+    assert np.array_equal(PIO.read_vec(tmp_path / "out_fields.pbvec"), rb[1])
+    assert np.array_equal(PIO.read_is(tmp_path / "out_pid.pbis"), rb[2])
+    with pytest.raises(RuntimeError, match="does not match"):
+        b.fill_from_files(tmp_path / "pcoor.pbvec", pid_file=tmp_path / "ppid_short.pbis") if (
+            PIO.write_is(tmp_path / "ppid_short.pbis", pid[:10]) or True) else None
+
+
 def test_error_paths():
     xd, fd, xp, opts = small_3d(np_=100)
     c = gpu_ctx(opts)
