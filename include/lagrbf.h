@@ -4,7 +4,7 @@
  *
  * Section 1 is the drop-in surface: the same eleven exported symbols, argument meaning and
  * error behaviour as LagRBF's ctypes interface (python_api/lagrbfpy/interface/register_cfunc.py:
- * 50-191; implementations in src/interface/*.c).  PetscInt is int32_t, PetscReal is double,
+ * 50-191; implementations in the src/interface/ C files).  PetscInt is int32_t, PetscReal is double,
  * PetscInt64 is int64_t and PetscErrorCode is int (0 = success).  `is_data` is declared bool,
  * which is how the ctypes binding passes it (register_cfunc.py:95,118).
  *
@@ -183,6 +183,46 @@ LAGRBF_EXPORT int lagrbf_fill_swarm_from_files(void *ctx, bool is_data, const ch
    <prefix>_pid.pbis, nglobal rows assembled by pid. */
 LAGRBF_EXPORT int lagrbf_output_files(void *ctx, bool is_data, int32_t nglobal, const char *prefix,
                                       const char *fieldname);
+
+/* ---------------------------------------------------------------------------------------- */
+/* 5. Serving loop (no counterpart in the reference)                                          */
+/* ---------------------------------------------------------------------------------------- */
+/* An advection job: the PU mesh and kernel of its dataset, the dataset itself (nd points, nfields
+   values each) or the id of a resident one, nsteps steps of size dt of the RK scheme
+   (0 RK1, 1 RK2, 2 RK4, 3 Dormand-Prince; CFL-limited inside each step like
+   lagrbf_advect_interpolate) on np particles.  Inputs are copied at submission. */
+typedef struct {
+  int32_t dim, nodes[3];
+  double O[3], L[3], overlap, shape_factor;
+  int32_t kernel, nfields;
+  int64_t dataset_id;     /* > 0: kept resident after the job under this id; 0: private */
+  int32_t nd;
+  const double *data_coords, *data_values; /* NULL for a resident dataset id */
+  int32_t np;
+  const double *particles;
+  int32_t scheme, nsteps;
+  double dt, cfl;          /* cfl <= 0: 0.3 */
+  int32_t fp32;            /* 1: FP32 evaluation */
+} lagrbf_job_t;
+typedef struct {
+  int64_t submitted, completed, failed, queued, running;
+  double p50_ms, p99_ms, mean_ms, max_ms; /* submission-to-completion latency of completed jobs */
+  double particle_steps, elapsed_s, bytes_in_use;
+  int32_t datasets_resident;
+} lagrbf_server_stats_t;
+/* Worker threads (one context and CUDA stream per running job) admit queued jobs first in, first
+   out as the device-memory budget and their dataset allow; a job may pass a waiting one that does
+   not fit yet, unless that one has waited over two seconds.  Idle resident datasets are evicted
+   least recently used first.  Latency is measured from submission. */
+LAGRBF_EXPORT void *lagrbf_server_create(double hbm_budget_bytes, int32_t nworkers);
+LAGRBF_EXPORT int lagrbf_server_submit(void *server, const lagrbf_job_t *job, int64_t *job_id);
+/* Blocks until the job is done; positions (nullable, np*dim) receive its particles by pid (rows of
+   particles that left the domain are zero). */
+LAGRBF_EXPORT int lagrbf_server_wait(void *server, int64_t job_id, double *positions, double *latency_ms);
+LAGRBF_EXPORT int lagrbf_server_stats(void *server, lagrbf_server_stats_t *stats);
+LAGRBF_EXPORT int lagrbf_server_reset_stats(void *server);
+/* Cancels queued jobs, lets running ones finish, frees every resident dataset. */
+LAGRBF_EXPORT void lagrbf_server_destroy(void *server);
 
 /* Binning without device allocation (no counterpart in the reference).  For callers that may not
    have a library allocate device memory at this point: a code running its time loop from a device

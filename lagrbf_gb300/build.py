@@ -17,7 +17,7 @@ LIB = os.path.join(HERE, "liblagrbf.so")
 
 CU_SOURCES = ["lgb_bin.cu", "lgb_eval32_3d.cu", "lgb_eval32_2d.cu", "lgb_eval64.cu", "lgb_factor.cu", "lgb_step.cu",
               "lgb_noalloc.cu"]
-C_SOURCES = ["lgb_host.c", "lgb_io.c"]
+C_SOURCES = ["lgb_host.c", "lgb_io.c", "lgb_serve.c"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # extra nvcc flags for tuning builds, e.g. LAGRBF_NVCC_FLAGS="-DLGB_X2_UNROLL=2" (default: none)
 EXTRA = os.environ.get("LAGRBF_NVCC_FLAGS", "").split()

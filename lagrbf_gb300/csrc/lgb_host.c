@@ -1486,3 +1486,23 @@ int lgb_ctx_dims(void *ctx, int *dim, int *nfields)
   *nfields = c->d.F;
   return 0;
 }
+
+/* Scheme and initial step of an existing context (the serving loop runs jobs with different RK
+   orders on one resident dataset). */
+int lgb_ctx_set_scheme(void *ctx, int scheme, double dt)
+{
+  lgb_ctx *c = (lgb_ctx *)ctx;
+  if (!c) return set_error(LAGRBF_ERR_ARG_NULL, "context is NULL");
+  if (scheme < 0 || scheme > 3) return set_error(LAGRBF_ERR_ARG_OUTOFRANGE, "unknown advection scheme %d", scheme);
+  CU(cudaMemcpyAsync(c->hctrl, c->d.ctrl, sizeof(lgb_ctrl), cudaMemcpyDeviceToHost, c->stream));
+  CU(cudaStreamSynchronize(c->stream));
+  c->scheme = scheme;
+  c->dt0 = dt;
+  c->hctrl->scheme = scheme;
+  c->hctrl->dt_adv = dt;
+  c->hctrl->dopri_error = DBL_MAX;
+  CU(cudaMemcpyAsync(c->d.ctrl, c->hctrl, sizeof(lgb_ctrl), cudaMemcpyHostToDevice, c->stream));
+  CU(cudaStreamSynchronize(c->stream));
+  invalidate_graph(c);
+  return 0;
+}
