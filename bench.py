@@ -49,6 +49,7 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--profile-only", action="store_true", help="setup + a few steps, for ncu")
     ap.add_argument("--quick", action="store_true", help="only the FP32 timed loop and the roofline pass")
+    ap.add_argument("--serve-jobs", type=int, default=60, help="jobs of the serving leg (0: skip it)")
     ap.add_argument("--solve-method", type=int, default=1,
                     help="1: A_KSP (factors resident), 2: A_KSP_ASMB (re-factor, no factor storage)")
     return ap.parse_args()
@@ -160,6 +161,35 @@ def run_reference(args):
             "e2e": {"value": v, "unit": "particle-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
     return 0
+
+
+def run_serving(njobs, workers=8, budget=150e9):
+    """The serving leg: a seeded Poisson stream (200 jobs/s offered) of advection jobs on six
+    datasets of 10K-2M nodes (30 % naming an already sent dataset), particle sets lognormal
+    around 100K, 1-50 steps of RK1/RK2/RK4/DP45, served under a 150 GB budget; latency from
+    submission to completion, aggregate particle-steps/s over the whole stream."""
+    from lagrbf_gb300 import workloads as W
+    from lagrbf_gb300.serving import Server
+    stream = W.serving_stream(np.random.default_rng(9), njobs=njobs, nd_range=(1e4, 2e6))
+    srv = Server(hbm_budget_bytes=budget, nworkers=workers)
+    t0 = time.perf_counter()
+    ids = []
+    for when, job in stream:
+        while time.perf_counter() - t0 < when:
+            time.sleep(0.0002)
+        ids.append(srv.submit(**job))
+    for i in ids:
+        srv.wait(i)
+    wall = time.perf_counter() - t0
+    st = srv.stats()
+    srv.close()
+    return {"p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"], "mean_ms": st["mean_ms"], "jobs": st["completed"],
+            "failed": st["failed"], "particle_steps_per_s": st["particle_steps"] / wall, "wall_s": wall,
+            "offered_jobs_per_s": 200.0, "workers": workers, "hbm_budget_gb": budget / 1e9,
+            "workload": "Poisson 200 jobs/s; 6 datasets 10K-2M nodes log-uniform (jittered lattice, 16-mode Fourier "
+                        "field, ~70 nodes per PU cell), "
+                        "30% reuse; particles lognormal median 100K in [1K, 4M]; 1-50 steps; RK1/RK2/RK4/DP45; "
+                        "FP32 evaluation; latency from submission"}
 
 
 def relerr_stats(a, b):
@@ -333,6 +363,10 @@ def main():
     barrier()
     ele = allmax(time.perf_counter() - ts)
     e2e = allsum(ctx.stats()["particle_steps"]) / ele
+    # ---------------- serving loop: Poisson stream of mixed advection jobs ----------------
+    serve = None
+    if rank == 0 and world == 1 and args.serve_jobs > 0:
+        serve = run_serving(args.serve_jobs)
     # ---------------- CPU baseline on the host cores ----------------
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -367,7 +401,7 @@ def main():
             "e2e": {"value": e2e, "unit": "particle-steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "steps": ke, "path": "fill_swarm(data) + lagrbf_interpolation + lagrbf_output + "
                                          "lagrbf_advect_interpolate, host numpy buffers"},
-            "roofline": roofline, "cpu_baseline": cpu, "clocks": clk, "gpu_launches": launches,
+            "roofline": roofline, "cpu_baseline": cpu, "clocks": clk, "gpu_launches": launches, "serve": serve,
         }
         print(json.dumps(line))
     if dist:

@@ -97,3 +97,38 @@ def config_precision_3d(nlat=80, npu=32, np_=4_000_000, seed=6):
     xp = uniform_points(np_, 3, np.random.default_rng(seed + 2))
     opts = dict(dim=3, npartitions=[npu] * 3, overlap=ov, shape_factor=float(nlat) / epsw, kernel=6, nfields=3)
     return xd, fd, xp, opts
+
+
+def serving_stream(rng, njobs=60, rate=200.0, ndatasets=6, nd_range=(1e4, 4e5), np_median=1e5,
+                   np_range=(1e3, 4e6), reuse=0.3, steps=(1, 50), dt=5e-4):
+    """Advection jobs for the serving loop: Poisson arrivals (rate jobs/s), datasets on jittered
+    lattices of log-uniform size carrying a 16-mode Fourier field (about 70 points per PU cell),
+    particle counts lognormal around np_median, RK order uniform in {1, 2, 4, DP45}, steps uniform.
+    A fraction `reuse` of the jobs names one of the datasets already sent; the data go with a
+    dataset's first job only.  Yields (arrival time, job keyword arguments)."""
+    dsets = []
+    for _ in range(ndatasets):
+        nd = float(np.exp(rng.uniform(np.log(nd_range[0]), np.log(nd_range[1]))))
+        nlat = max(8, int(round(nd ** (1.0 / 3.0))))
+        xd = jittered_lattice(nlat, 3, rng)
+        fd = fourier_field(xd, rng, nmodes=16)
+        npu = max(3, int(round((len(xd) / 70.0) ** (1.0 / 3.0))) + 1)
+        dsets.append((xd, fd, npu))
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, size=njobs))
+    sent = set()
+    out = []
+    for k in range(njobs):
+        if sent and rng.uniform() < reuse:
+            which = int(rng.choice(sorted(sent)))
+        else:
+            which = int(rng.integers(0, ndatasets))
+        xd, fd, npu = dsets[which]
+        n = int(np.clip(np.exp(rng.normal(np.log(np_median), 1.0)), np_range[0], np_range[1]))
+        job = dict(npartitions=[npu] * 3, particles=rng.uniform(0.0, 1.0, (n, 3)), dt=dt,
+                   nsteps=int(rng.integers(steps[0], steps[1] + 1)), scheme=int(rng.integers(0, 4)), fp32=True,
+                   dataset_id=which + 1)
+        if which not in sent:
+            job.update(data_coords=xd, data_values=fd)
+            sent.add(which)
+        out.append((float(arrivals[k]), job))
+    return out
