@@ -48,7 +48,8 @@ __device__ __forceinline__ const double *lcol(const double *L, int m, int j)
    and solved by one warp with shuffles, the block's solution is kept in shared memory (Y, 4 x 32),
    and the rest of the patch is updated by all threads, each factor element read once per block
    for all four right-hand sides.  The forward sweep subtracts L(i, j) y_j in ascending j for every
-   row, as a column sweep does. */
+   row, as a column sweep does; the diagonal divisions are multiplications by reciprocals computed
+   once per block. */
 template <bool PACKED>
 __device__ __forceinline__ long long lbase(int m, int j)
 {
@@ -80,12 +81,15 @@ __device__ void chol_solve_blocked(const double *L, int m, int F, double *B, dou
         double v[4];
 #pragma unroll
         for (int q = 0; q < 4; q++) v[q] = (q < fc && lane < nb) ? B0[(size_t)q * m + j0 + lane] : 0.0;
+        /* reciprocal of this lane's diagonal element, once: a division per step and right-hand
+           side, executed by the whole warp, would load the FP64 pipe more than the updates do */
+        const double rl = (lane < nb) ? 1.0 / D[lane * 33 + lane] : 0.0;
         for (int jj = 0; jj < nb; jj++) {
-          const double d = D[jj * 33 + jj];
+          const double rj = __shfl_sync(0xffffffffu, rl, jj);
           const double l = (lane > jj && lane < nb) ? D[lane * 33 + jj] : 0.0;
 #pragma unroll
           for (int q = 0; q < 4; q++) {
-            const double y = __shfl_sync(0xffffffffu, v[q], jj) / d;
+            const double y = __shfl_sync(0xffffffffu, v[q], jj) * rj;
             if (lane == jj) v[q] = y;
             else if (lane > jj) v[q] -= l * y;
           }
@@ -148,12 +152,13 @@ __device__ void chol_solve_blocked(const double *L, int m, int F, double *B, dou
         double v[4];
 #pragma unroll
         for (int q = 0; q < 4; q++) v[q] = (q < fc && lane < nb) ? B0[(size_t)q * m + i0 + lane] : 0.0;
+        const double rl = (lane < nb) ? 1.0 / D[lane * 33 + lane] : 0.0;
         for (int ii = nb - 1; ii >= 0; ii--) {
-          const double d = D[ii * 33 + ii];
+          const double ri = __shfl_sync(0xffffffffu, rl, ii);
           const double l = (lane < ii) ? D[ii * 33 + lane] : 0.0;
 #pragma unroll
           for (int q = 0; q < 4; q++) {
-            const double x = __shfl_sync(0xffffffffu, v[q], ii) / d;
+            const double x = __shfl_sync(0xffffffffu, v[q], ii) * ri;
             if (lane == ii) v[q] = x;
             else if (lane < ii) v[q] -= l * x;
           }
