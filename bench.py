@@ -192,6 +192,32 @@ def run_serving(njobs, workers=8, budget=150e9):
                         "FP32 evaluation; latency from submission"}
 
 
+def run_precision_stress(np_=1_000_000):
+    """The precision-stress configuration at 1M particles: 80^3 jittered lattice, Gaussian kernel
+    with eps_r = 1/h (h the lattice spacing), 16 seeded Fourier modes with amplitudes ~N(0,1)/k^2,
+    32^3 PU nodes; FP32 evaluation against the all-FP64 path on the same factors' data, max and RMS
+    relative error per component, plus the FP64 interpolant against the exact field."""
+    import lagrbf_gb300 as L
+    from lagrbf_gb300 import workloads as W
+    xd, fd, xp, opts = W.config_precision_3d(np_=np_)
+    res = {}
+    for prec in ("fp64", "fp32"):
+        c = L.LagRBFCtx(**opts, solve_method=1, eval_precision=prec)
+        c.fill_data(xd, fd)
+        c.fill_points(xp)
+        c.interpolate_c()
+        f = np.zeros((np_, 3))
+        c.output(fvals=f)
+        res[prec] = f
+        del c
+    mx, rms = relerr_stats(res["fp32"], res["fp64"])
+    exact = W.fourier_field(xp, np.random.default_rng(7))
+    ex_mx, ex_rms = relerr_stats(res["fp64"], exact)
+    return {"workload": "80^3 jittered lattice, Gaussian eps_r = 1/h, 16 Fourier modes, 32^3 PU, %d particles" % np_,
+            "fp32_vs_fp64_max_rel_err": mx, "fp32_vs_fp64_rms_rel_err": rms,
+            "fp64_vs_exact_max_rel_err": ex_mx, "fp64_vs_exact_rms_rel_err": ex_rms}
+
+
 def relerr_stats(a, b):
     den = np.abs(b).max(axis=0)
     den[den == 0] = 1.0
@@ -350,11 +376,12 @@ def main():
     ctx.fill_points(x_start[alive], values=f_start[alive], pidx=p_start[alive])
     h2d = xd.nbytes + fd.nbytes
     d2h = xo.nbytes + fo.nbytes + po.nbytes
+    fd_alt = (fd, fd * (1.0 + 1e-6))  # the nodal field changes every step, as in a coupled run
     ctx.reset_stats()
     barrier()
     ts = time.perf_counter()
-    for _ in range(ke):
-        ctx.fill_data(xd, fd)
+    for k in range(ke):
+        ctx.fill_data(xd, fd_alt[k % 2])
         ctx.interpolate_c()
         ctx.output(coords=xo, fvals=fo, pidx=po)
         ctx.advect_interpolate_c(t, t + DT)
@@ -363,6 +390,10 @@ def main():
     barrier()
     ele = allmax(time.perf_counter() - ts)
     e2e = allsum(ctx.stats()["particle_steps"]) / ele
+    # ---------------- precision stress (Gaussian, small shape parameter) ----------------
+    precision = None
+    if rank == 0 and world == 1 and args.serve_jobs > 0:
+        precision = run_precision_stress()
     # ---------------- serving loop: Poisson stream of mixed advection jobs ----------------
     serve = None
     if rank == 0 and world == 1 and args.serve_jobs > 0:
@@ -399,9 +430,11 @@ def main():
                      "fp32_vs_fp64_max_abs_pos_err": pos_err,
                      "err_definition": "per component: max_p|a-b| / max_p|b| and RMS(a-b)/RMS(b), fields after 1 step"},
             "e2e": {"value": e2e, "unit": "particle-steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                    "steps": ke, "path": "fill_swarm(data) + lagrbf_interpolation + lagrbf_output + "
+                    "steps": ke, "path": "fill_swarm(data, nodal values changing every step) + lagrbf_interpolation "
+                                         "(all patch coefficients re-solved) + lagrbf_output + "
                                          "lagrbf_advect_interpolate, host numpy buffers"},
             "roofline": roofline, "cpu_baseline": cpu, "clocks": clk, "gpu_launches": launches, "serve": serve,
+            "precision_stress": precision,
         }
         print(json.dumps(line))
     if dist:
