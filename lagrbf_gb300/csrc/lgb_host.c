@@ -1112,10 +1112,8 @@ static int do_output(lgb_ctx *c, int is_data, int nglobal, double *coords, doubl
     if (err) { rc = set_error(LAGRBF_ERR_MEM, "output scratch allocation failed"); goto done; }
     OP(lgb_op_output_rows(n, c->pidd, d->alive, nglobal, c->out_inv, c->out_bad, dim, d->xp, coords, nf, src, fields,
                           (long long *)pidx, d->nsm, c->stream));
-    CU(cudaMemcpyAsync(&c->hctrl->eval_error, c->out_bad, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    CU(cudaMemcpyAsync(&bad, c->out_bad, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
     CU(cudaStreamSynchronize(c->stream));
-    bad = c->hctrl->eval_error;
-    c->hctrl->eval_error = 0;
     if (bad) rc = set_error(LAGRBF_ERR_ARG_OUTOFRANGE, "a particle pid is out of range [1, %d]", nglobal);
     goto done;
   }
