@@ -92,8 +92,14 @@ LAGRBF_EXPORT int lagrbf_options_set_value(const char *name, const char *value)
       return 0;
     }
   if (g_nopts == g_capopts) {
-    g_capopts = g_capopts ? 2 * g_capopts : 32;
-    g_opts = (opt_t *)realloc(g_opts, sizeof(opt_t) * (size_t)g_capopts);
+    int cap = g_capopts ? 2 * g_capopts : 32;
+    opt_t *no = (opt_t *)realloc(g_opts, sizeof(opt_t) * (size_t)cap);
+    if (!no) {
+      pthread_mutex_unlock(&g_optlock);
+      return set_error(LAGRBF_ERR_MEM, "out of host memory");
+    }
+    g_opts = no;
+    g_capopts = cap;
   }
   g_opts[g_nopts].key = strdup(name);
   g_opts[g_nopts].val = strdup(value ? value : "");

@@ -255,9 +255,13 @@ static void *worker(void *arg)
       ctx = d->ctx;
     } else if (cached) {
       if (s->nds == s->capds) {
-        s->capds = s->capds ? 2 * s->capds : 16;
-        s->ds = (srv_dataset *)realloc(s->ds, sizeof(srv_dataset) * (size_t)s->capds);
+        int cap = s->capds ? 2 * s->capds : 16;
+        srv_dataset *nd = (srv_dataset *)realloc(s->ds, sizeof(srv_dataset) * (size_t)cap);
+        if (nd) { s->ds = nd; s->capds = cap; }
       }
+      if (s->nds == s->capds) cached = 0; /* no room in the table: run it as a private dataset */
+    }
+    if (!d && cached) {
       d = &s->ds[s->nds++];
       memset(d, 0, sizeof(*d));
       d->id = j->spec.dataset_id;
@@ -293,10 +297,11 @@ static void *worker(void *arg)
     if (rc) s->failed++;
     else {
       if (s->nlat == s->caplat) {
-        s->caplat = s->caplat ? 2 * s->caplat : 1024;
-        s->lat = (double *)realloc(s->lat, sizeof(double) * (size_t)s->caplat);
+        int64_t cap = s->caplat ? 2 * s->caplat : 1024;
+        double *nl = (double *)realloc(s->lat, sizeof(double) * (size_t)cap);
+        if (nl) { s->lat = nl; s->caplat = cap; }
       }
-      s->lat[s->nlat++] = 1e3 * (j->t_done - j->t_submit);
+      if (s->nlat < s->caplat) s->lat[s->nlat++] = 1e3 * (j->t_done - j->t_submit);
       s->pss += j->pss;
       s->t_last = j->t_done;
     }
@@ -376,8 +381,15 @@ LAGRBF_EXPORT int lagrbf_server_submit(void *srv, const lagrbf_job_t *job, int64
   }
   pthread_mutex_lock(&s->lock);
   if (s->njobs == s->capjobs) {
-    s->capjobs = s->capjobs ? 2 * s->capjobs : 1024;
-    s->jobs = (srv_job **)realloc(s->jobs, sizeof(srv_job *) * (size_t)s->capjobs);
+    int64_t cap = s->capjobs ? 2 * s->capjobs : 1024;
+    srv_job **nj = (srv_job **)realloc(s->jobs, sizeof(srv_job *) * (size_t)cap);
+    if (!nj) {
+      pthread_mutex_unlock(&s->lock);
+      free(j->xd); free(j->fd); free(j->xp); free(j->result); free(j);
+      return lgb_set_error_msg(LAGRBF_ERR_MEM, "out of host memory");
+    }
+    s->jobs = nj;
+    s->capjobs = cap;
   }
   s->jobs[s->njobs] = j;
   j->id = ++s->njobs;
