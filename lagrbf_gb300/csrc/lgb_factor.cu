@@ -20,6 +20,7 @@
 #include "lgb_common.cuh"
 
 #define FACT_T 256
+#define CHOL_NB 16 /* columns per Cholesky panel */
 
 struct FactorParams {
   lgb_geom g;
@@ -229,27 +230,65 @@ __global__ void __launch_bounds__(FACT_T) k_factor(FactorParams P)
         }
       }
       __syncthreads();
-      /* left-looking Cholesky */
-      for (int j = 0; j < m; j++) {
-        const double *Lj = A + j; /* row j: Lj[k*m] = L(j,k) */
-        for (int i = j + tid; i < m; i += FACT_T) {
-          double s = A[(size_t)j * m + i];
-          for (int k = 0; k < j; k++) s -= A[(size_t)k * m + i] * Lj[(size_t)k * m];
-          A[(size_t)j * m + i] = s;
-        }
-        __syncthreads();
-        double dd = A[(size_t)j * m + j];
-        if (!(dd > 0.0)) {
-          if (tid == 0) {
-            if (atomicCAS(&P.ctrl->factor_error, 0, j + 1) == 0) P.ctrl->factor_node = node;
-            s_fail = 1;
+      /* Cholesky in panels of CHOL_NB columns: each panel is factored left-looking from the
+         entries already updated by the earlier panels, then the trailing lower triangle is updated
+         by the panel (tiles of 32 x 32, one warp per tile).  Every entry receives its updates
+         -L(i,k) L(j,k) one at a time in ascending k, exactly as in an unblocked left-looking
+         factorisation, so the factor is the same bit for bit; the blocking only stops each column
+         from re-reading all earlier columns. */
+      double *Ps = B + (size_t)m * F; /* panel rows [p0, m) x CHOL_NB, stride CHOL_NB + 1 */
+      for (int p0 = 0; p0 < m && !s_fail; p0 += CHOL_NB) {
+        const int nb = min(CHOL_NB, m - p0), p1 = p0 + nb;
+        for (int j = p0; j < p1; j++) {
+          const double *Lj = A + j; /* row j: Lj[k*m] = L(j,k) */
+          for (int i = j + tid; i < m; i += FACT_T) {
+            double s = A[(size_t)j * m + i];
+            for (int k = p0; k < j; k++) s -= A[(size_t)k * m + i] * Lj[(size_t)k * m];
+            A[(size_t)j * m + i] = s;
           }
-          break;
+          __syncthreads();
+          double dd = A[(size_t)j * m + j];
+          if (!(dd > 0.0)) {
+            if (tid == 0) {
+              if (atomicCAS(&P.ctrl->factor_error, 0, j + 1) == 0) P.ctrl->factor_node = node;
+              s_fail = 1;
+            }
+            break;
+          }
+          dd = sqrt(dd);
+          for (int i = j + 1 + tid; i < m; i += FACT_T) A[(size_t)j * m + i] /= dd;
+          __syncthreads();
+          if (tid == 0) A[(size_t)j * m + j] = dd;
+          __syncthreads();
         }
-        dd = sqrt(dd);
-        for (int i = j + 1 + tid; i < m; i += FACT_T) A[(size_t)j * m + i] /= dd;
         __syncthreads();
-        if (tid == 0) A[(size_t)j * m + j] = dd;
+        if (s_fail || p1 >= m) break;
+        /* stage the panel's rows (row-major, padded) for the trailing update */
+        for (int t = tid; t < (m - p0) * nb; t += FACT_T) {
+          const int kk = t / (m - p0), r = t - kk * (m - p0);
+          Ps[(size_t)r * (CHOL_NB + 1) + kk] = A[(size_t)(p0 + kk) * m + p0 + r];
+        }
+        __syncthreads();
+        const int T = (m - p1 + 31) / 32, ntile = T * (T + 1) / 2;
+        const int lane = tid & 31, warp = tid >> 5;
+        for (int t = warp; t < ntile; t += FACT_T / 32) {
+          int c = 0, rem = t;
+          while (rem >= T - c) { rem -= T - c; c++; }
+          const int i = p1 + 32 * (c + rem) + lane, jb = p1 + 32 * c;
+          if (i >= m) continue;
+          double li[CHOL_NB];
+#pragma unroll
+          for (int kk = 0; kk < CHOL_NB; kk++) li[kk] = (kk < nb) ? Ps[(size_t)(i - p0) * (CHOL_NB + 1) + kk] : 0.0;
+          const int jend = min(jb + 32, i + 1);
+          for (int j = jb; j < jend; j++) {
+            const double *lj = Ps + (size_t)(j - p0) * (CHOL_NB + 1);
+            double a = A[(size_t)j * m + i];
+#pragma unroll
+            for (int kk = 0; kk < CHOL_NB; kk++)
+              if (kk < nb) a -= li[kk] * lj[kk];
+            A[(size_t)j * m + i] = a;
+          }
+        }
         __syncthreads();
       }
       __syncthreads();

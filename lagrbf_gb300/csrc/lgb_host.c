@@ -565,7 +565,7 @@ static int ensure_pools(lgb_ctx *c)
   /* factorisation workspace: per slot m^2 + m*(dim+F) doubles, up to 4 slots per SM within ~4 GB */
   {
     long long m = d->max_patch > 0 ? d->max_patch : 1;
-    long long stride = m * m + m * (d->g.dim + d->F) + 32;
+    long long stride = m * m + m * (d->g.dim + d->F) + m * 17 + 32; /* + Cholesky panel rows */
     long long budget = 4LL << 30;
     int nws = 4 * d->nsm; /* four patches per SM in flight: the solves are latency bound */
     if ((long long)nws * stride * 8 > budget) nws = (int)(budget / (stride * 8));
