@@ -142,10 +142,10 @@ static inline double phi_lane(int kernel, double r, double eps)
   case ORC_KERNEL_LINEAR: return eps * r;
   case ORC_KERNEL_WENDLAND_C0: u = 1.0 - eps * r; if (!(u >= 0.0)) u = 0.0; return u * u;
   case ORC_KERNEL_WENDLAND_C2:
+    /* the mask select of the vector form, without a branch (so loops over lanes stay loops) */
     u = 1.0 - eps * r;
-    if (!(u >= 0.0)) return 0.0;
     u2 = u * u; u4 = u2 * u2; inner = 5.0 - 4.0 * u;
-    return u4 * inner;
+    return (u >= 0.0) ? u4 * inner : 0.0;
   case ORC_KERNEL_BUMP:
     u = 1.0 - eps * r;
     if (!(u >= 0.0)) return 0.0;
@@ -265,35 +265,44 @@ long orc_block_csr(const orc_pu *pu, const int *cell_start, const int *cell_pts,
 /* ======================================================================================= */
 /* PU weights: SwarmInterpSetWeights_AVX256 (weights_avx.c:97-243)                          */
 /* ======================================================================================= */
-static inline double wdist_lane(const orc_pu *pu, const double *x, int node)
+/* Node coordinates as the DMDA coordinate vector holds them (LA_coords, weights_avx.c:122-125):
+   node n = ix + iy*nx + iz*nx*ny at O + h*i per axis (partition_of_unity.c:143). */
+static double *node_table(const orc_pu *pu)
 {
-  int ix = node % pu->n[0];
-  int iy = (node / pu->n[0]) % pu->n[1];
-  int iz = node / (pu->n[0] * pu->n[1]);
-  double dx = x[0] - node_coord(pu, 0, ix);
-  double dy = x[1] - node_coord(pu, 1, iy);
-  if (pu->dim == 2) return sqrt(fma(dx, dx, dy * dy));
+  int n, d;
+  double *t = (double *)malloc(sizeof(double) * (size_t)pu->dim * (size_t)pu->nnodes);
+  if (!t) return NULL;
+  for (n = 0; n < pu->nnodes; n++) {
+    int idx[3];
+    idx[0] = n % pu->n[0];
+    idx[1] = (n / pu->n[0]) % pu->n[1];
+    idx[2] = n / (pu->n[0] * pu->n[1]);
+    for (d = 0; d < pu->dim; d++) t[(size_t)pu->dim * n + d] = node_coord(pu, d, idx[d]);
+  }
+  return t;
+}
+
+static inline double wdist_lane(int dim, const double *x, const double *c)
+{
+  double dx = x[0] - c[0], dy = x[1] - c[1];
+  if (dim == 2) return sqrt(fma(dx, dx, dy * dy));
   {
-    double dz = x[2] - node_coord(pu, 2, iz);
+    double dz = x[2] - c[2];
     return sqrt(fma(dx, dx, fma(dy, dy, dz * dz)));
   }
 }
 
-static inline double wdist_scalar(const orc_pu *pu, const double *x, int node)
+static inline double wdist_scalar(int dim, const double *x, const double *c)
 {
-  int idx[3], d;
+  int d;
   double dist = 0.0;
-  idx[0] = node % pu->n[0];
-  idx[1] = (node / pu->n[0]) % pu->n[1];
-  idx[2] = node / (pu->n[0] * pu->n[1]);
-  for (d = 0; d < pu->dim; d++) {
-    double c = node_coord(pu, d, idx[d]);
-    dist += (x[d] - c) * (x[d] - c);
-  }
+  for (d = 0; d < dim; d++) dist += (x[d] - c[d]) * (x[d] - c[d]);
   return sqrt(dist);
 }
 
-static void weights_one(const orc_pu *pu, const double *x, int cell, double *w)
+static inline __attribute__((always_inline)) void weights_one_d(const orc_pu *pu, const int dim,
+                                                                 const double *ntab, const double *x, int cell,
+                                                                 double *w)
 {
   int nen = pu->nen, k, n, l;
   int corners[8];
@@ -302,7 +311,8 @@ static void weights_one(const orc_pu *pu, const double *x, int cell, double *w)
   for (k = 0; k < nen; k++) corners[k] = orc_cell_corner(pu, cell, k);
   for (n = 0; n < aligned; n += 4) {
     double wa[4];
-    for (l = 0; l < 4; l++) wa[l] = phi_lane(ORC_KERNEL_WENDLAND_C2, wdist_lane(pu, x, n + l), pu->eps_w);
+    for (l = 0; l < 4; l++)
+      wa[l] = phi_lane(ORC_KERNEL_WENDLAND_C2, wdist_lane(dim, x, &ntab[(size_t)dim * (n + l)]), pu->eps_w);
     sum_w += wa[0] + wa[1] + wa[2] + wa[3];
     for (k = 0; k < nen; k++) {
       int nd = corners[k];
@@ -313,7 +323,7 @@ static void weights_one(const orc_pu *pu, const double *x, int cell, double *w)
     }
   }
   for (; n < pu->nnodes; n++) {
-    double weight = orc_phi_scalar(ORC_KERNEL_WENDLAND_C2, wdist_scalar(pu, x, n), pu->eps_w);
+    double weight = orc_phi_scalar(ORC_KERNEL_WENDLAND_C2, wdist_scalar(dim, x, &ntab[(size_t)dim * n]), pu->eps_w);
     sum_w += weight;
     for (k = 0; k < nen; k++) if (corners[k] == n) { w[k] = weight; break; }
   }
@@ -323,15 +333,24 @@ static void weights_one(const orc_pu *pu, const double *x, int cell, double *w)
   }
 }
 
+static void weights_one(const orc_pu *pu, const double *ntab, const double *x, int cell, double *w)
+{
+  if (pu->dim == 2) weights_one_d(pu, 2, ntab, x, cell, w);
+  else weights_one_d(pu, 3, ntab, x, cell, w);
+}
+
 void orc_weights(const orc_pu *pu, int np, const double *coords, const int *cellid, const int *alive,
                  double *weights)
 {
   int p;
+  double *ntab = node_table(pu);
+  if (!ntab) return;
   for (p = 0; p < np; p++) {
     if (alive && !alive[p]) continue;
     if (cellid[p] < 0) continue;
-    weights_one(pu, &coords[pu->dim * p], cellid[p], &weights[pu->nen * p]);
+    weights_one(pu, ntab, &coords[pu->dim * p], cellid[p], &weights[pu->nen * p]);
   }
+  free(ntab);
 }
 
 /* ======================================================================================= */
@@ -445,29 +464,30 @@ int orc_patch_solve(const orc_pu *pu, int kernel, int m, const int *idx, const d
 /* ======================================================================================= */
 /* evaluation: PointwiseInterpolation_AVX512 (interpolation_avx512.c:121-291)               */
 /* ======================================================================================= */
-static void eval_one(const orc_pu *pu, int kernel, const double *x, int cell, const double *w,
-                     const double *xd, const int *blk_start, const int *blk_pts, const int *patch_start,
-                     const int *patch_pts, const int *patch_setup, double *const *coeffs, int nf,
-                     double *rbf_d, double *val)
+static inline __attribute__((always_inline)) void
+eval_one_k(const orc_pu *pu, const int dim, const int kernel, const double *x, int cell, const double *w,
+           const double *restrict xd, const int *blk_start, const int *blk_pts, const int *patch_start,
+           const int *patch_pts, const int *patch_setup, double *const *coeffs, int nf, double *restrict rbf_d,
+           double *val)
 {
-  int dim = pu->dim, nen = pu->nen, k, f, nd, i;
+  int nen = pu->nen, k, f, nd, i;
   int bs = blk_start[cell], bn = blk_start[cell + 1] - bs;
   const int *bidx = &blk_pts[bs];
   int aligned;
   double eps = pu->eps_r;
   if (bn == 0) return; /* interpolation_avx512.c:184: the value is left untouched */
   aligned = (bn / 8) * 8;
-  for (nd = 0; nd < aligned; nd += 8)
+  for (nd = 0; nd < aligned; nd += 8) {
+    double r[8];
     for (i = 0; i < 8; i++) {
       int dp = bidx[nd + i];
-      double dx = x[0] - xd[dim * dp], dy = x[1] - xd[dim * dp + 1], dist2;
-      if (dim == 2) dist2 = fma(dx, dx, dy * dy);
-      else {
-        double dz = x[2] - xd[dim * dp + 2];
-        dist2 = fma(dx, dx, fma(dy, dy, dz * dz));
-      }
-      rbf_d[dp] = phi_lane(kernel, sqrt(dist2), eps);
+      double dx = x[0] - xd[dim * dp], dy = x[1] - xd[dim * dp + 1];
+      double dz = (dim == 3) ? x[2] - xd[dim * dp + 2] : 0.0;
+      r[i] = sqrt((dim == 3) ? fma(dx, dx, fma(dy, dy, dz * dz)) : fma(dx, dx, dy * dy));
     }
+    for (i = 0; i < 8; i++) r[i] = phi_lane(kernel, r[i], eps);
+    for (i = 0; i < 8; i++) rbf_d[bidx[nd + i]] = r[i];
+  }
   for (nd = aligned; nd < bn; nd++) {
     int dp = bidx[nd], d;
     double dist = 0.0;
@@ -481,19 +501,25 @@ static void eval_one(const orc_pu *pu, int kernel, const double *x, int cell, co
     const int *didx = &patch_pts[ps];
     const double *c = coeffs[node];
     int al;
-    double interp[64];
+    double interp[64], acc[8 * 64];
     if (!patch_setup[node] || m == 0 || !c) continue; /* ndata == 0 when the patch is not set up */
     al = (m / 8) * 8;
-    for (f = 0; f < nf; f++) {
-      double l[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-      const double *cf = &c[(size_t)f * m];
-      for (nd = 0; nd < al; nd += 8)
-        for (i = 0; i < 8; i++) l[i] = fma(rbf_d[didx[nd + i]], cf[nd + i], l[i]);
-      /* horizontal sum: 512 -> 256 (lo+hi), 256 -> 128 (lo+hi), hadd */
-      {
-        double s0 = l[0] + l[4], s1 = l[1] + l[5], s2 = l[2] + l[6], s3 = l[3] + l[7];
-        interp[f] = (s0 + s2) + (s1 + s3);
+    /* eight lanes per field; the eight phi values are gathered once for all fields */
+    for (f = 0; f < 8 * nf; f++) acc[f] = 0.0;
+    for (nd = 0; nd < al; nd += 8) {
+      double r[8];
+      for (i = 0; i < 8; i++) r[i] = rbf_d[didx[nd + i]];
+      for (f = 0; f < nf; f++) {
+        const double *cf = &c[(size_t)f * m + nd];
+        double *l = &acc[8 * f];
+        for (i = 0; i < 8; i++) l[i] = fma(r[i], cf[i], l[i]);
       }
+    }
+    for (f = 0; f < nf; f++) {
+      /* horizontal sum: 512 -> 256 (lo+hi), 256 -> 128 (lo+hi), hadd */
+      const double *l = &acc[8 * f];
+      double s0 = l[0] + l[4], s1 = l[1] + l[5], s2 = l[2] + l[6], s3 = l[3] + l[7];
+      interp[f] = (s0 + s2) + (s1 + s3);
     }
     for (nd = al; nd < m; nd++) {
       double rbf = rbf_d[didx[nd]];
@@ -501,6 +527,32 @@ static void eval_one(const orc_pu *pu, int kernel, const double *x, int cell, co
     }
     for (f = 0; f < nf; f++) val[f] += interp[f] * w[k];
   }
+}
+
+/* eval_one_k with the kernel and the dimension as constants: the reference picks its kernel and
+   distance functions once per call (function pointers, interpolation_avx512.c:150-172), so the
+   per-element kernel switch of phi_lane is hoisted out of the loops here too. */
+static void eval_one(const orc_pu *pu, int kernel, const double *x, int cell, const double *w,
+                     const double *xd, const int *blk_start, const int *blk_pts, const int *patch_start,
+                     const int *patch_pts, const int *patch_setup, double *const *coeffs, int nf,
+                     double *rbf_d, double *val)
+{
+  if (nf < 1 || nf > 64) return; /* per-field scratch of eval_one_k */
+#define ORC_EVAL_K(D, K) eval_one_k(pu, D, K, x, cell, w, xd, blk_start, blk_pts, patch_start, patch_pts, \
+                                    patch_setup, coeffs, nf, rbf_d, val)
+  if (pu->dim == 3) {
+    switch (kernel) {
+    case ORC_KERNEL_WENDLAND_C2: ORC_EVAL_K(3, ORC_KERNEL_WENDLAND_C2); return;
+    case ORC_KERNEL_GAUSSIAN: ORC_EVAL_K(3, ORC_KERNEL_GAUSSIAN); return;
+    default: ORC_EVAL_K(3, kernel); return;
+    }
+  }
+  switch (kernel) {
+  case ORC_KERNEL_WENDLAND_C2: ORC_EVAL_K(2, ORC_KERNEL_WENDLAND_C2); return;
+  case ORC_KERNEL_GAUSSIAN: ORC_EVAL_K(2, ORC_KERNEL_GAUSSIAN); return;
+  default: ORC_EVAL_K(2, kernel); return;
+  }
+#undef ORC_EVAL_K
 }
 
 static void eval_all(const orc_pu *pu, int kernel, int np, const double *xp, const int *cellid, const int *alive,
@@ -577,6 +629,7 @@ orc_ctx *orc_create(const orc_config *cfg)
   orc_ctx *c;
   int n;
   if (cfg->dim != 2 && cfg->dim != 3) return NULL; /* cell_info.c:312-324 */
+  if (cfg->nfields < 1 || cfg->nfields > 64) return NULL;
   for (n = 0; n < cfg->dim; n++) if (cfg->n[n] < 2) return NULL;
   c = (orc_ctx *)calloc(1, sizeof(*c));
   c->cfg = *cfg;
