@@ -12,8 +12,10 @@
  * reads of a column are coalesced and the pivot row is a broadcast), then the F right-hand sides
  * are solved together.  FP64 throughout: the collocation systems are ill-conditioned.  A
  * non-positive pivot sets ctrl->factor_error (1-based row) and leaves the patch not set up; no
- * trap, no abort.  When factors are kept (A_FACTOR / A_KSP) the factor is packed (column-major
- * lower, m(m+1)/2) so that new field values only need the two triangular solves.
+ * trap, no abort.  The factor is then "prepared" for the solves (reciprocal diagonal and scaled
+ * diagonal blocks, below); when factors are kept (A_FACTOR / A_KSP) it is packed (column-major
+ * lower, m(m+1)/2) so that new field values only need the two triangular solves, which run the same
+ * code on the same values as the first solve.
  *
  * Roofline: FP64 pipe (m^3/3 flops per patch); workspace traffic stays in L2 for m <= ~700.
  */
@@ -36,21 +38,9 @@ struct FactorParams {
   lgb_ctrl *ctrl;
 };
 
-/* Column j of the lower factor from its diagonal element down: packed column-major (m(m+1)/2,
-   the kept factors) or the full column-major workspace.  L(i, j) = lcol(j)[i - j], i >= j. */
-template <bool PACKED>
-__device__ __forceinline__ const double *lcol(const double *L, int m, int j)
-{
-  return PACKED ? L + ((long long)j * m - ((long long)j * (j - 1)) / 2) : L + (size_t)j * m + j;
-}
 
-/* Solves L L^T X = B in place for the F columns of B (B[f*m + i]), in blocks of 32 rows and four
-   right-hand sides at a time: the 32 x 32 diagonal block is staged in shared memory (D, 32 x 33)
-   and solved by one warp with shuffles, the block's solution is kept in shared memory (Y, 4 x 32),
-   and the rest of the patch is updated by all threads, each factor element read once per block
-   for all four right-hand sides.  The forward sweep subtracts L(i, j) y_j in ascending j for every
-   row, as a column sweep does; the diagonal divisions are multiplications by reciprocals computed
-   once per block. */
+/* Column j of the lower factor from its diagonal element down: packed column-major (m(m+1)/2,
+   the kept factors) or the full column-major workspace.  L(i, j) = L[lbase(j) + (i - j)]. */
 template <bool PACKED>
 __device__ __forceinline__ long long lbase(int m, int j)
 {
@@ -62,113 +52,144 @@ __device__ __forceinline__ long long lstep(int m, int j)
   return PACKED ? (long long)(m - j) : (long long)m + 1; /* base(j + 1) - base(j) */
 }
 
+/* The factor as the solves read it ("prepared"): the 32 x 32 diagonal blocks hold the reciprocal
+   1 / L(j, j) on the diagonal and M(i, j) = L(i, j) / L(j, j) below it; every other entry is
+   L(i, j).  With M the substitutions inside a diagonal block are fused multiply-adds only:
+     forward   u_i = b_i - sum_{k<i} M(i,k) u_k,              y_i = u_i / L(i,i)
+     backward  w_i = y_i / L(i,i) - sum_{k>i} M(k,i) x_k,      x_i = w_i
+   (L(i,k) y_k = M(i,k) u_k and L(k,i) x_k / L(i,i) = M(k,i) x_k), which halves the FP64
+   instructions of the block substitutions, the serial part of the solve. */
 template <bool PACKED>
-__device__ void chol_solve_blocked(const double *L, int m, int F, double *B, double *D, double *Y)
+__device__ void prepare_diag_blocks(double *L, int m)
 {
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarp = blockDim.x >> 5;
+  for (int j = threadIdx.x; j < m; j += blockDim.x) {
+    const long long b = lbase<PACKED>(m, j);
+    const double d = L[b];
+    const int iend = min((j / 32 + 1) * 32, m);
+    for (int i = j + 1; i < iend; i++) L[b + (i - j)] /= d;
+  }
+  __syncthreads();
+  for (int j = threadIdx.x; j < m; j += blockDim.x) {
+    const long long b = lbase<PACKED>(m, j);
+    L[b] = 1.0 / L[b];
+  }
+  __syncthreads();
+}
+
+/* D[r * 33 + c] = prepared diagonal block entry (j0 + r, j0 + c), r >= c; column-wise reads. */
+template <bool PACKED>
+__device__ __forceinline__ void stage_diag(const double *L, int m, int j0, int nb, double *D)
+{
+  for (int t = threadIdx.x; t < nb * nb; t += blockDim.x) {
+    const int c = t / nb, r = t - c * nb;
+    if (r >= c) D[r * 33 + c] = L[lbase<PACKED>(m, j0 + c) + (r - c)];
+  }
+}
+
+/* Solves L L^T X = B in place for FC (1..4) columns of B (B[q*m + i]) with the prepared factor,
+   in blocks of 32 rows.  Each diagonal block is staged in shared memory (D, 32 x 33) and
+   substituted by one warp with shuffles, every lane issuing the same fused multiply-add (zero
+   multiplier where a lane has nothing to subtract); the block's solution is kept in shared memory
+   (Y, 4 x 32) and the other rows are updated by all threads, each factor element read once per
+   block for all FC right-hand sides.  Forward: rows below the block, L(i, j) read down columns
+   (coalesced).  Backward: rows above the block, x_i -= sum_r L(i0 + r, i) x_r, each thread
+   reading 32 consecutive entries of its own column.  Only FP64 fused multiply-adds and one
+   multiplication per block and right-hand side; no reductions. */
+template <bool PACKED, int FC>
+__device__ void chol_solve_group(const double *__restrict__ L, int m, double *B0, double *D, double *Y)
+{
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int nblk = (m + 31) / 32;
-  for (int f0 = 0; f0 < F; f0 += 4) {
-    const int fc = min(4, F - f0);
-    double *B0 = B + (size_t)f0 * m;
-    /* forward: L y = b */
-    for (int kb = 0; kb < nblk; kb++) {
-      const int j0 = kb * 32, nb = min(32, m - j0);
-      for (int t = tid; t < nb * nb; t += blockDim.x) {
-        const int r = t / nb, c = t - r * nb;
-        if (r >= c) D[r * 33 + c] = L[lbase<PACKED>(m, j0 + c) + (r - c)];
+  for (int kb = 0; kb < nblk; kb++) {
+    const int j0 = kb * 32, nb = min(32, m - j0);
+    stage_diag<PACKED>(L, m, j0, nb, D);
+    __syncthreads();
+    if (warp == 0) {
+      double u[FC];
+#pragma unroll
+      for (int q = 0; q < FC; q++) u[q] = (lane < nb) ? B0[(size_t)q * m + j0 + lane] : 0.0;
+      for (int jj = 0; jj < nb - 1; jj++) {
+        const double mij = (lane > jj && lane < nb) ? D[lane * 33 + jj] : 0.0;
+#pragma unroll
+        for (int q = 0; q < FC; q++) u[q] = fma(-mij, __shfl_sync(0xffffffffu, u[q], jj), u[q]);
       }
-      __syncthreads();
-      if (warp == 0) {
-        double v[4];
+      const double rl = (lane < nb) ? D[lane * 33 + lane] : 0.0;
 #pragma unroll
-        for (int q = 0; q < 4; q++) v[q] = (q < fc && lane < nb) ? B0[(size_t)q * m + j0 + lane] : 0.0;
-        /* reciprocal of this lane's diagonal element, once: a division per step and right-hand
-           side, executed by the whole warp, would load the FP64 pipe more than the updates do */
-        const double rl = (lane < nb) ? 1.0 / D[lane * 33 + lane] : 0.0;
-        for (int jj = 0; jj < nb; jj++) {
-          const double rj = __shfl_sync(0xffffffffu, rl, jj);
-          const double l = (lane > jj && lane < nb) ? D[lane * 33 + jj] : 0.0;
-#pragma unroll
-          for (int q = 0; q < 4; q++) {
-            const double y = __shfl_sync(0xffffffffu, v[q], jj) * rj;
-            if (lane == jj) v[q] = y;
-            else if (lane > jj) v[q] -= l * y;
-          }
-        }
-#pragma unroll
-        for (int q = 0; q < 4; q++) {
-          Y[q * 32 + lane] = v[q];
-          if (q < fc && lane < nb) B0[(size_t)q * m + j0 + lane] = v[q];
-        }
+      for (int q = 0; q < FC; q++) {
+        const double y = u[q] * rl;
+        Y[q * 32 + lane] = y;
+        if (lane < nb) B0[(size_t)q * m + j0 + lane] = y;
       }
-      __syncthreads();
-      const long long b0 = lbase<PACKED>(m, j0);
-      for (int i = j0 + nb + tid; i < m; i += blockDim.x) {
-        double acc[4];
-#pragma unroll
-        for (int q = 0; q < 4; q++) acc[q] = (q < fc) ? B0[(size_t)q * m + i] : 0.0;
-        long long cb = b0 - j0; /* element (i, j) of column j at cb + i */
-#pragma unroll 8
-        for (int jj = 0; jj < nb; jj++) {
-          const double l = L[cb + i - jj];
-#pragma unroll
-          for (int q = 0; q < 4; q++)
-            if (q < fc) acc[q] -= l * Y[q * 32 + jj];
-          cb += lstep<PACKED>(m, j0 + jj);
-        }
-#pragma unroll
-        for (int q = 0; q < 4; q++)
-          if (q < fc) B0[(size_t)q * m + i] = acc[q];
-      }
-      __syncthreads();
     }
-    /* backward: L^T x = y, blocks from the bottom */
-    for (int kb = nblk - 1; kb >= 0; kb--) {
-      const int i0 = kb * 32, nb = min(32, m - i0), k1 = i0 + nb;
-      /* y_i -= sum_{k >= k1} L(k, i) x_k for the block's rows: one warp per row */
-      for (int r = warp; r < nb; r += nwarp) {
-        const int i = i0 + r;
-        const double *ci = L + lbase<PACKED>(m, i) - i; /* L(k, i) = ci[k] */
-        double part[4] = {0.0, 0.0, 0.0, 0.0};
-#pragma unroll 4
-        for (int k = k1 + lane; k < m; k += 32) {
-          const double l = ci[k];
+    __syncthreads();
+    const long long b0 = lbase<PACKED>(m, j0);
+    for (int i = j0 + nb + tid; i < m; i += blockDim.x) {
+      double acc[FC];
 #pragma unroll
-          for (int q = 0; q < 4; q++)
-            if (q < fc) part[q] += l * B0[(size_t)q * m + k];
-        }
+      for (int q = 0; q < FC; q++) acc[q] = B0[(size_t)q * m + i];
+      long long cb = b0 - j0; /* element (i, j) of column j at cb + i */
+#pragma unroll 8
+      for (int jj = 0; jj < nb; jj++) {
+        const double l = L[cb + i - jj];
 #pragma unroll
-        for (int q = 0; q < 4; q++) {
-          double pq = part[q];
-          for (int off = 16; off > 0; off >>= 1) pq += __shfl_down_sync(0xffffffffu, pq, off);
-          if (lane == 0 && q < fc) B0[(size_t)q * m + i] -= pq;
-        }
+        for (int q = 0; q < FC; q++) acc[q] = fma(-l, Y[q * 32 + jj], acc[q]);
+        cb += lstep<PACKED>(m, j0 + jj);
       }
-      for (int t = tid; t < nb * nb; t += blockDim.x) {
-        const int r = t / nb, c = t - r * nb;
-        if (r >= c) D[r * 33 + c] = L[lbase<PACKED>(m, i0 + c) + (r - c)];
+#pragma unroll
+      for (int q = 0; q < FC; q++) B0[(size_t)q * m + i] = acc[q];
+    }
+    __syncthreads();
+  }
+  for (int kb = nblk - 1; kb >= 0; kb--) {
+    const int i0 = kb * 32, nb = min(32, m - i0);
+    stage_diag<PACKED>(L, m, i0, nb, D);
+    __syncthreads();
+    if (warp == 0) {
+      const double rl = (lane < nb) ? D[lane * 33 + lane] : 0.0;
+      double w[FC];
+#pragma unroll
+      for (int q = 0; q < FC; q++) w[q] = ((lane < nb) ? B0[(size_t)q * m + i0 + lane] : 0.0) * rl;
+      for (int ii = nb - 1; ii >= 1; ii--) {
+        const double mi = (lane < ii) ? D[ii * 33 + lane] : 0.0;
+#pragma unroll
+        for (int q = 0; q < FC; q++) w[q] = fma(-mi, __shfl_sync(0xffffffffu, w[q], ii), w[q]);
       }
-      __syncthreads();
-      if (warp == 0) {
-        double v[4];
 #pragma unroll
-        for (int q = 0; q < 4; q++) v[q] = (q < fc && lane < nb) ? B0[(size_t)q * m + i0 + lane] : 0.0;
-        const double rl = (lane < nb) ? 1.0 / D[lane * 33 + lane] : 0.0;
-        for (int ii = nb - 1; ii >= 0; ii--) {
-          const double ri = __shfl_sync(0xffffffffu, rl, ii);
-          const double l = (lane < ii) ? D[ii * 33 + lane] : 0.0;
-#pragma unroll
-          for (int q = 0; q < 4; q++) {
-            const double x = __shfl_sync(0xffffffffu, v[q], ii) * ri;
-            if (lane == ii) v[q] = x;
-            else if (lane < ii) v[q] -= l * x;
-          }
-        }
-#pragma unroll
-        for (int q = 0; q < 4; q++)
-          if (q < fc && lane < nb) B0[(size_t)q * m + i0 + lane] = v[q];
+      for (int q = 0; q < FC; q++) {
+        Y[q * 32 + lane] = w[q];
+        if (lane < nb) B0[(size_t)q * m + i0 + lane] = w[q];
       }
-      __syncthreads();
+    }
+    __syncthreads();
+    for (int i = tid; i < i0; i += blockDim.x) {
+      double acc[FC];
+#pragma unroll
+      for (int q = 0; q < FC; q++) acc[q] = B0[(size_t)q * m + i];
+      const double *ci = L + lbase<PACKED>(m, i) + (i0 - i); /* L(i0 + r, i) = ci[r] */
+#pragma unroll 8
+      for (int r = 0; r < nb; r++) {
+        const double l = ci[r];
+#pragma unroll
+        for (int q = 0; q < FC; q++) acc[q] = fma(-l, Y[q * 32 + r], acc[q]);
+      }
+#pragma unroll
+      for (int q = 0; q < FC; q++) B0[(size_t)q * m + i] = acc[q];
+    }
+    __syncthreads();
+  }
+}
+
+/* All F right-hand sides of B (B[f*m + i]), four at a time. */
+template <bool PACKED>
+__device__ void chol_solve(const double *L, int m, int F, double *B, double *D, double *Y)
+{
+  for (int f0 = 0; f0 < F; f0 += 4) {
+    double *B0 = B + (size_t)f0 * m;
+    switch (min(4, F - f0)) {
+    case 1: chol_solve_group<PACKED, 1>(L, m, B0, D, Y); break;
+    case 2: chol_solve_group<PACKED, 2>(L, m, B0, D, Y); break;
+    case 3: chol_solve_group<PACKED, 3>(L, m, B0, D, Y); break;
+    default: chol_solve_group<PACKED, 4>(L, m, B0, D, Y); break;
     }
   }
 }
@@ -293,6 +314,7 @@ __global__ void __launch_bounds__(FACT_T) k_factor(FactorParams P)
       }
       __syncthreads();
       if (s_fail) { __syncthreads(); continue; }
+      prepare_diag_blocks<false>(A, m);
       if (P.keep) {
         double *Fk = P.fac + P.foff[node];
         for (int j = 0; j < m; j++) {
@@ -309,8 +331,8 @@ __global__ void __launch_bounds__(FACT_T) k_factor(FactorParams P)
     }
     __syncthreads();
     if (m > 0) {
-      if (have_factor) chol_solve_blocked<true>(P.fac + P.foff[node], m, F, B, s_diag, s_y);
-      else chol_solve_blocked<false>(A, m, F, B, s_diag, s_y);
+      if (have_factor) chol_solve<true>(P.fac + P.foff[node], m, F, B, s_diag, s_y);
+      else chol_solve<false>(A, m, F, B, s_diag, s_y);
       /* coefficients [point][field] in both precisions */
       const long long c0 = P.coff[node];
       for (int q = tid; q < m; q += FACT_T)

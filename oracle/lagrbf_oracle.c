@@ -537,7 +537,7 @@ static void eval_one(const orc_pu *pu, int kernel, const double *x, int cell, co
                      const int *patch_pts, const int *patch_setup, double *const *coeffs, int nf,
                      double *rbf_d, double *val)
 {
-  if (nf < 1 || nf > 64) return; /* per-field scratch of eval_one_k */
+  if (nf < 1 || nf > 64) return; /* nothing to evaluate / per-field scratch of eval_one_k */
 #define ORC_EVAL_K(D, K) eval_one_k(pu, D, K, x, cell, w, xd, blk_start, blk_pts, patch_start, patch_pts, \
                                     patch_setup, coeffs, nf, rbf_d, val)
   if (pu->dim == 3) {
@@ -629,7 +629,7 @@ orc_ctx *orc_create(const orc_config *cfg)
   orc_ctx *c;
   int n;
   if (cfg->dim != 2 && cfg->dim != 3) return NULL; /* cell_info.c:312-324 */
-  if (cfg->nfields < 1 || cfg->nfields > 64) return NULL;
+  if (cfg->nfields < 0 || cfg->nfields > 64) return NULL; /* per-field scratch of the evaluation */
   for (n = 0; n < cfg->dim; n++) if (cfg->n[n] < 2) return NULL;
   c = (orc_ctx *)calloc(1, sizeof(*c));
   c->cfg = *cfg;

@@ -141,3 +141,15 @@ def test_rk_convergence_order(scheme, order):
 
 def test_dopri_meets_tolerance():
     assert _rotation_error(3, 0.1) <= 1e-6
+
+
+def test_analytical_advection_without_fields():
+    """n_interpolation_fields = 0 is a valid configuration for analytical advection."""
+    xp = np.array([[0.3, 0.5], [0.6, 0.4]])
+    o = Oracle(dim=2, npartitions=[5, 5], nfields=0, overlap=W.pu_overlap(5), kernel=2, advection=True,
+               advection_scheme=2, advection_cfl=0.2)
+    assert o.set_velocity_batch(_rotation_batch) == 0
+    assert o.fill(False, xp) == 0
+    assert o.advect_analytical(0.0, 0.3) == 0
+    x, _, _ = o.output(len(xp), fieldname="velocity")
+    assert np.all(np.isfinite(x)) and np.abs(x - xp).max() > 0.0
