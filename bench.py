@@ -374,7 +374,7 @@ def main():
     ke = args.e2e_steps or args.steps
     xo = np.zeros((npart, 3)); fo = np.zeros((npart, 3)); po = np.zeros(npart, dtype=np.int64)
     ctx.fill_points(x_start[alive], values=f_start[alive], pidx=p_start[alive])
-    h2d = xd.nbytes + fd.nbytes
+    h2d = fd.nbytes  # the coordinates are the same every step: compared on the host, not sent again
     d2h = xo.nbytes + fo.nbytes + po.nbytes
     fd_alt = (fd, fd * (1.0 + 1e-6))  # the nodal field changes every step, as in a coupled run
     ctx.reset_stats()
@@ -430,7 +430,8 @@ def main():
                      "fp32_vs_fp64_max_abs_pos_err": pos_err,
                      "err_definition": "per component: max_p|a-b| / max_p|b| and RMS(a-b)/RMS(b), fields after 1 step"},
             "e2e": {"value": e2e, "unit": "particle-steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                    "steps": ke, "path": "fill_swarm(data, nodal values changing every step) + lagrbf_interpolation "
+                    "steps": ke, "path": "fill_swarm(data: same coordinates, compared word for word on the host and not "
+                                         "sent again; nodal values changing every step) + lagrbf_interpolation "
                                          "(all patch coefficients re-solved) + lagrbf_output + "
                                          "lagrbf_advect_interpolate, host numpy buffers"},
             "roofline": roofline, "cpu_baseline": cpu, "clocks": clk, "gpu_launches": launches, "serve": serve,

@@ -419,18 +419,41 @@ __global__ void k_pid_inverse(int n, const long long *__restrict__ pid, const in
   inv[gi] = p;
 }
 
-__global__ void k_output_rows(int nglobal, const int *__restrict__ inv, int dim, const double *__restrict__ x,
-                              double *coords, int nf, const double *__restrict__ src, double *fields,
-                              const long long *__restrict__ pid, long long *pidx)
+/* Output rows gi of the caller's arrays (often pageable host memory reached through the GPU's
+   address translation): a CTA gathers the rows of a tile of OUT_ROWS particles into shared memory,
+   then writes each array's tile as one contiguous span, consecutive threads on consecutive words,
+   so that every store fills whole sectors instead of a stride-dim pattern. */
+#define OUT_ROWS 256
+#define OUT_MAXW 8 /* words per row staged: dim <= 3, nf <= 8; wider rows are written directly */
+__global__ void __launch_bounds__(OUT_ROWS) k_output_rows(int nglobal, const int *__restrict__ inv, int dim,
+                                                          const double *__restrict__ x, double *coords, int nf,
+                                                          const double *__restrict__ src, double *fields,
+                                                          const long long *__restrict__ pid, long long *pidx)
 {
-  for (long long gi = blockIdx.x * (long long)blockDim.x + threadIdx.x; gi < nglobal;
-       gi += (long long)gridDim.x * blockDim.x) {
-    const int p = inv[gi];
-    if (coords)
-      for (int d = 0; d < dim; d++) coords[gi * dim + d] = (p >= 0) ? x[(size_t)p * dim + d] : 0.0;
-    if (fields)
-      for (int f = 0; f < nf; f++) fields[gi * nf + f] = (p >= 0) ? src[(size_t)p * nf + f] : 0.0;
-    if (pidx) pidx[gi] = (p >= 0) ? pid[p] : 0;
+  __shared__ double s_row[OUT_ROWS * OUT_MAXW];
+  const int t = threadIdx.x;
+  for (long long g0 = (long long)blockIdx.x * OUT_ROWS; g0 < nglobal; g0 += (long long)gridDim.x * OUT_ROWS) {
+    const int nr = (int)min((long long)OUT_ROWS, (long long)nglobal - g0);
+    const long long gi = g0 + t;
+    const int p = (t < nr) ? inv[gi] : -1;
+    if (pidx && t < nr) pidx[gi] = (p >= 0) ? pid[p] : 0;
+    for (int a = 0; a < 2; a++) {
+      const int w = a ? nf : dim;
+      const double *in = a ? src : x;
+      double *out = a ? fields : coords;
+      if (!out || w <= 0) continue;
+      if (w > OUT_MAXW) {
+        if (t < nr)
+          for (int k = 0; k < w; k++) out[gi * w + k] = (p >= 0) ? in[(size_t)p * w + k] : 0.0;
+        continue;
+      }
+      if (t < nr)
+        for (int k = 0; k < w; k++) s_row[t * w + k] = (p >= 0) ? in[(size_t)p * w + k] : 0.0;
+      __syncthreads();
+      double *o = out + g0 * w;
+      for (int e = t; e < nr * w; e += OUT_ROWS) o[e] = s_row[e];
+      __syncthreads();
+    }
   }
 }
 
@@ -443,9 +466,9 @@ extern "C" int lgb_op_output_rows(int n, const long long *pid, const int *alive,
   cudaMemsetAsync(bad, 0, sizeof(int), s);
   if (n > 0) k_pid_inverse<<<lgb_cdiv(n, 256), 256, 0, s>>>(n, pid, alive, nglobal, inv, bad);
   if (nglobal > 0) {
-    int grid = lgb_cdiv(nglobal, 256);
+    int grid = lgb_cdiv(nglobal, OUT_ROWS);
     if (grid > 8 * nsm) grid = 8 * nsm;
-    k_output_rows<<<grid, 256, 0, s>>>(nglobal, inv, dim, x, coords, nf, src, fields, pid, pidx);
+    k_output_rows<<<grid, OUT_ROWS, 0, s>>>(nglobal, inv, dim, x, coords, nf, src, fields, pid, pidx);
   }
   lgb_count_launch(2);
   return (int)cudaGetLastError();

@@ -660,7 +660,9 @@ static int fill_data(lgb_ctx *c, int n, const double *coords, const double *valu
   }
   if (n > old && F > 0) CU(cudaMemsetAsync(d->fd + (size_t)old * F, 0, sizeof(double) * (size_t)(n - old) * F, c->stream));
   d->nd = n;
-  if (n > 0) CU(cudaMemcpyAsync(d->xd, coords, sizeof(double) * (size_t)n * dim, cudaMemcpyHostToDevice, c->stream));
+  /* unchanged coordinates (compared word for word above) are already on the device */
+  if (n > 0 && !same_coords)
+    CU(cudaMemcpyAsync(d->xd, coords, sizeof(double) * (size_t)n * dim, cudaMemcpyHostToDevice, c->stream));
   if (values && n > 0 && F > 0)
     CU(cudaMemcpyAsync(d->fd, values, sizeof(double) * (size_t)n * F, cudaMemcpyHostToDevice, c->stream));
   if (same_coords) {

@@ -407,3 +407,52 @@ def test_graph_and_eager_paths_agree():
         c.advect_interpolate_c(0.0, 0.02)
         outs.append(gpu_output(c, len(xp), 3))
     assert np.array_equal(outs[0][0], outs[1][0]) and np.array_equal(outs[0][1], outs[1][1])
+
+
+@pytest.mark.parametrize("solve_method", [0, 1])
+@pytest.mark.parametrize("reset", [True, False])
+def test_refill_same_coordinates_new_values(solve_method, reset):
+    """Data refilled with the same coordinates and new values, as a coupled run does between steps:
+    the coordinates are not sent again and the kept factors (A_KSP) are reused.  As in the
+    reference, solved patches keep their coefficients until lagrbf_reset_coefficients (or the
+    end-of-call reset of the advection) marks them unsolved; GPU and oracle follow the same call
+    sequence."""
+    xd, fd, xp, opts = small_3d(np_=1500)
+    fd2 = W.fourier_field(xd, np.random.default_rng(3))
+    c = gpu_ctx(opts, solve_method=solve_method)
+    o = Oracle(**opts, solve_method=solve_method)
+    c.fill_data(xd, fd); c.fill_points(xp); c.interpolate_c()
+    assert o.fill(True, xd, fd) == 0 and o.fill(False, xp) == 0 and o.interpolate() == 0
+    nfac = c.stats()["patches_factored"]
+    if reset:
+        c.reset_coefficients(); o.reset()
+    c.fill_data(xd.copy(), fd2); c.interpolate_c()
+    assert o.fill(True, xd, fd2) == 0 and o.interpolate() == 0
+    if solve_method == 1:
+        assert c.stats()["patches_factored"] == nfac
+    x1, f1, p1 = gpu_output(c, len(xp), opts["nfields"])
+    x2, f2, p2 = o.output(len(xp))
+    assert np.array_equal(p1, p2) and np.array_equal(x1, x2)
+    assert relerr(f1, f2) <= TOL64
+    if reset:
+        fresh = Oracle(**opts, solve_method=solve_method)
+        assert fresh.fill(True, xd, fd2) == 0 and fresh.fill(False, xp) == 0 and fresh.interpolate() == 0
+        assert relerr(f1, fresh.output(len(xp))[1]) <= TOL64
+
+
+def test_output_rows_wider_than_staging():
+    """Rows of more than eight fields are written without the shared-memory staging and equal the
+    host-assembled copy; nine fields also take the solve's four-, four- and one-column groups."""
+    xd, _, xp, opts = small_3d(np_=600)
+    fd = np.concatenate([W.fourier_field(xd, np.random.default_rng(s)) for s in range(4)], axis=1)[:, :9]
+    opts = dict(opts, nfields=9)
+    outs = []
+    for direct in (True, False):
+        c = gpu_ctx(opts, output_direct=direct)
+        c.fill_data(xd, fd); c.fill_points(xp); c.interpolate_c()
+        outs.append(gpu_output(c, len(xp), 9))
+    for a, b in zip(*outs):
+        assert np.array_equal(a, b)
+    o = Oracle(**opts)
+    assert o.fill(True, xd, fd) == 0 and o.fill(False, xp) == 0 and o.interpolate() == 0
+    assert relerr(outs[0][1], o.output(len(xp))[1]) <= TOL64
