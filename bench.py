@@ -50,6 +50,7 @@ def parse():
     ap.add_argument("--profile-only", action="store_true", help="setup + a few steps, for ncu")
     ap.add_argument("--quick", action="store_true", help="only the FP32 timed loop and the roofline pass")
     ap.add_argument("--serve-jobs", type=int, default=60, help="jobs of the serving leg (0: skip it)")
+    ap.add_argument("--uneven", type=int, default=1, help="run the uneven-mixture leg (0: skip it)")
     ap.add_argument("--solve-method", type=int, default=1,
                     help="1: A_KSP (factors resident), 2: A_KSP_ASMB (re-factor, no factor storage)")
     return ap.parse_args()
@@ -190,6 +191,43 @@ def run_serving(njobs, workers=8, budget=150e9):
                         "field, ~70 nodes per PU cell), "
                         "30% reuse; particles lognormal median 100K in [1K, 4M]; 1-50 steps; RK1/RK2/RK4/DP45; "
                         "FP32 evaluation; latency from submission"}
+
+
+def run_uneven(rk4_steps=3, dopri_steps=5):
+    """The uneven configuration: 1M points (90 % from 8 Gaussians of widths 0.02-0.2, 10 % uniform),
+    ABC flow, 8M particles from the same mixture, Wendland C2 on a uniform 160^3 PU mesh (largest
+    patch 1,713 points, 2.3M non-empty patches).  Set-up time, then FP32-evaluation RK4 steps at
+    the CFL step and Dormand-Prince steps (rtol 1e-6, atol 1e-9, global adapted step) over an
+    interval of about `dopri_steps` of the step adapted by a first call."""
+    import lagrbf_gb300 as L
+    from lagrbf_gb300 import workloads as W
+    xd, fd, xp, opts = W.config_uneven_3d()
+    out = {"workload": "uneven: 1M-point Gaussian mixture + 10% uniform, ABC flow, 160^3 PU, Wendland C2, "
+                       "8M particles from the mixture, FP32 evaluation"}
+    for scheme, name in ((2, "rk4"), (3, "dopri")):
+        c = L.LagRBFCtx(**opts, advection=True, advection_scheme=scheme, advection_cfl=0.3, solve_method=1,
+                        eval_precision="fp32", dt=DT, petsc_options={"dopri_rtol": 1e-6, "dopri_atol": 1e-9})
+        c.synchronize()
+        ts = time.perf_counter()
+        c.fill_data(xd, fd); c.fill_points(xp); c.interpolate_c(); c.synchronize()
+        if scheme == 2:
+            st = c.stats()
+            out.update(setup_s=time.perf_counter() - ts, max_patch=st["max_patch"],
+                       patches_factored=st["patches_factored"])
+        t = 0.0
+        c.advect_resident(t, t + 1e-5); t += 1e-5  # warm-up (and the first adapted step for DOPRI)
+        c.synchronize()
+        span = rk4_steps * DT if scheme == 2 else dopri_steps * c.stats()["dt"]
+        c.reset_stats()
+        ts = time.perf_counter()
+        c.advect_resident(t, t + span)
+        c.synchronize()
+        el = time.perf_counter() - ts
+        st = c.stats()
+        out[name] = {"value": st["particle_steps"] / el, "unit": "particle-steps/s", "steps": st["steps"],
+                     "dt_last": st["dt"], "seconds": el}
+        del c
+    return out
 
 
 def run_precision_stress(np_=1_000_000):
@@ -395,6 +433,9 @@ def main():
     if rank == 0 and world == 1 and args.serve_jobs > 0:
         precision = run_precision_stress()
     # ---------------- serving loop: Poisson stream of mixed advection jobs ----------------
+    uneven = None
+    if rank == 0 and world == 1 and args.uneven:
+        uneven = run_uneven()
     serve = None
     if rank == 0 and world == 1 and args.serve_jobs > 0:
         serve = run_serving(args.serve_jobs)
@@ -434,8 +475,12 @@ def main():
                                          "sent again; nodal values changing every step) + lagrbf_interpolation "
                                          "(all patch coefficients re-solved) + lagrbf_output + "
                                          "lagrbf_advect_interpolate, host numpy buffers"},
+            "with_setup": {"value": ps_total / el_max * (50 * el_max / args.steps) /
+                           (setup_s + 50 * el_max / args.steps), "unit": "particle-steps/s", "steps": 50,
+                           "definition": "50 RK4 steps including the one-time set-up (binning, factorisation, "
+                                         "first solve): particles x 50 / (setup_s + 50 x the timed step)"},
             "roofline": roofline, "cpu_baseline": cpu, "clocks": clk, "gpu_launches": launches, "serve": serve,
-            "precision_stress": precision,
+            "precision_stress": precision, "uneven": uneven,
         }
         print(json.dumps(line))
     if dist:

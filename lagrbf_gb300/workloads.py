@@ -43,9 +43,16 @@ def uniform_points(n, dim, rng):
     return np.ascontiguousarray(rng.uniform(0.0, 1.0, (n, dim)))
 
 
-def mixture_points(n, dim, rng, nclusters=8, background=0.1):
-    centres = rng.uniform(0.2, 0.8, (nclusters, dim))
-    sig = rng.uniform(0.02, 0.2, nclusters)
+def mixture_clusters(dim, rng, nclusters=8):
+    """Centres U[0.2, 0.8]^dim and widths U[0.02, 0.2] of an isotropic Gaussian mixture."""
+    return rng.uniform(0.2, 0.8, (nclusters, dim)), rng.uniform(0.02, 0.2, nclusters)
+
+
+def mixture_points(n, dim, rng, nclusters=8, background=0.1, clusters=None):
+    """n points: a fraction `background` uniform on [0,1]^dim, the rest from the mixture (draws
+    outside [0,1]^dim rejected); `clusters` = (centres, widths) reuses a mixture."""
+    centres, sig = clusters if clusters is not None else mixture_clusters(dim, rng, nclusters)
+    nclusters = len(sig)
     nb = int(n * background)
     out = [rng.uniform(0, 1, (nb, dim))]
     need = n - nb
@@ -83,6 +90,20 @@ def config_abc_3d(nlat=128, npu=32, np_=16_777_216, seed=3):
     xd = jittered_lattice(nlat, 3, rng)
     fd = abc_flow(xd)
     xp = uniform_points(np_, 3, np.random.default_rng(seed + 1))
+    opts = dict(dim=3, npartitions=[npu] * 3, overlap=pu_overlap(npu), shape_factor=1.0, kernel=2, nfields=3)
+    return xd, fd, xp, opts
+
+
+def config_uneven_3d(nd=1_000_000, npu=160, np_=8_000_000, seed=5):
+    """3D uneven data: 90 % of the points from 8 isotropic Gaussians (widths 0.02-0.2) and 10 %
+    uniform, ABC flow, particles from the same mixture; Wendland C2 on a uniform npu^3 PU mesh.
+    The PU mesh is fine enough that the densest patch stays a dense system of a few thousand
+    points (npu = 160, seed 5: largest patch 1,713 points, 2.3 M non-empty patches)."""
+    rng = np.random.default_rng(seed)
+    clusters = mixture_clusters(3, rng)
+    xd = mixture_points(nd, 3, rng, clusters=clusters)
+    fd = abc_flow(xd)
+    xp = mixture_points(np_, 3, np.random.default_rng(seed + 1), clusters=clusters)
     opts = dict(dim=3, npartitions=[npu] * 3, overlap=pu_overlap(npu), shape_factor=1.0, kernel=2, nfields=3)
     return xd, fd, xp, opts
 

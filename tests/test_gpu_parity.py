@@ -456,3 +456,34 @@ def test_output_rows_wider_than_staging():
     o = Oracle(**opts)
     assert o.fill(True, xd, fd) == 0 and o.fill(False, xp) == 0 and o.interpolate() == 0
     assert relerr(outs[0][1], o.output(len(xp))[1]) <= TOL64
+
+
+@pytest.mark.parametrize("scheme", [2, 3])
+def test_uneven_mixture_matches_oracle(scheme):
+    """Uneven data and particles (Gaussian mixture): cells holding several work units of particles,
+    patches from a few points to 925, RK4 and Dormand-Prince with the global adapted step."""
+    xd, fd, xp, opts = W.config_uneven_3d(nd=10000, npu=24, np_=15000, seed=5)
+    nc = opts["npartitions"][0] - 1
+    cx = np.minimum((xp * nc).astype(int), nc - 1)
+    per_cell = np.bincount(cx[:, 0] + nc * (cx[:, 1] + nc * cx[:, 2]), minlength=nc ** 3)
+    assert per_cell.max() > 2 * 256  # more particles in a cell than the largest work unit
+    adv = dict(advection=True, advection_scheme=scheme, advection_cfl=0.3, solve_method=1)
+    c = gpu_ctx(opts, **adv)
+    o = Oracle(**opts, **adv)
+    c.fill_points(xp)
+    assert o.fill(False, xp) == 0
+    t, dt = 0.0, 5e-3
+    for _ in range(2):
+        # the advection loop clears the data swarm at its end: refill, as a coupled run does
+        c.fill_data(xd, fd); c.interpolate_c()
+        assert o.fill(True, xd, fd) == 0 and o.interpolate() == 0
+        c.advect_interpolate_c(t, t + dt)
+        assert o.advect(t, t + dt) == 0
+        t += dt
+    x1, f1, p1 = gpu_output(c, len(xp), 3)
+    x2, f2, p2 = o.output(len(xp))
+    assert np.array_equal(p1, p2)
+    assert np.abs(x1 - x2).max() <= 1e-12
+    assert relerr(f1, f2) <= TOL64
+    if scheme == 3:
+        assert abs(c.stats()["dt"] - o.dt()) <= 1e-9 * abs(o.dt())
