@@ -49,6 +49,8 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--profile-only", action="store_true", help="setup + a few steps, for ncu")
     ap.add_argument("--quick", action="store_true", help="only the FP32 timed loop and the roofline pass")
+    ap.add_argument("--profile-solve", action="store_true",
+                    help="setup, reset_coefficients, one re-solve of every patch (kept factors), for ncu")
     ap.add_argument("--serve-jobs", type=int, default=60, help="jobs of the serving leg (0: skip it)")
     ap.add_argument("--uneven", type=int, default=1, help="run the uneven-mixture leg (0: skip it)")
     ap.add_argument("--solve-method", type=int, default=1,
@@ -314,6 +316,17 @@ def main():
     ctx.synchronize()
     setup_s = time.perf_counter() - t0
     st0 = ctx.stats()
+    if args.profile_solve:
+        ctx.reset_coefficients()
+        ctx.set_profiling(True)
+        ctx.reset_stats()
+        ctx.interpolate_c()
+        ctx.synchronize()
+        sp = ctx.stats()
+        print(json.dumps({"profile_solve": True, "setup_s": setup_s, "solve_ms": sp["factor_ms"],
+                          "solve_fp64_tflops": sp["factor_flops"] / (sp["factor_ms"] * 1e-3) / 1e12,
+                          "max_patch": sp["max_patch"], "patches": sp["npatch_setup"]}))
+        return 0
     if args.profile_only:
         for s in range(max(args.steps, 1)):
             ctx.advect_resident(s * DT, (s + 1) * DT)
@@ -415,6 +428,12 @@ def main():
     h2d = fd.nbytes  # the coordinates are the same every step: compared on the host, not sent again
     d2h = xo.nbytes + fo.nbytes + po.nbytes
     fd_alt = (fd, fd * (1.0 + 1e-6))  # the nodal field changes every step, as in a coupled run
+    for k in range(args.warmup):  # untimed warm-up steps (first touch of the caller's output arrays)
+        ctx.fill_data(xd, fd_alt[k % 2])
+        ctx.interpolate_c()
+        ctx.output(coords=xo, fvals=fo, pidx=po)
+        ctx.advect_interpolate_c(t, t + DT)
+        t += DT
     ctx.reset_stats()
     barrier()
     ts = time.perf_counter()

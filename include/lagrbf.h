@@ -91,8 +91,9 @@ LAGRBF_EXPORT void lagrbf_interpolate_driver(int32_t ndata_local, double *data_c
    advection_scheme, velocity_name, dt, cfl_fac, rmin, rmax, dopri_dt_fac, dopri_dt_fac_min,
    dopri_dt_fac_max, dopri_atol, dopri_rtol; and the GPU-only keys eval_precision (fp64|fp32,
    default fp64), use_cuda_graph (bool, default true), cuda_device (int), output_direct (bool,
-   default true: lagrbf_output's particle rows are written by the GPU straight into the caller's
-   arrays when the device accesses pageable host memory).  Arrays are comma separated. */
+   default true: when the device accesses pageable host memory, lagrbf_output's particle rows are
+   written by the GPU straight into the caller's arrays and lagrbf_fill_swarm's data arrays are
+   read by it directly).  Arrays are comma separated. */
 LAGRBF_EXPORT int lagrbf_options_set_value(const char *name, const char *value);
 LAGRBF_EXPORT int lagrbf_options_clear(void);
 LAGRBF_EXPORT int lagrbf_options_insert_file(const char *path);

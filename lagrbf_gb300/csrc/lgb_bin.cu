@@ -473,3 +473,32 @@ extern "C" int lgb_op_output_rows(int n, const long long *pid, const int *alive,
   lgb_count_launch(2);
   return (int)cudaGetLastError();
 }
+
+/* Host-to-device copy by the device itself, for host arrays it reads directly: 16-byte loads when
+   both ends are 16-byte aligned, else 8-byte loads; consecutive threads on consecutive words. */
+__global__ void k_copy_in(double *__restrict__ dst, const double *__restrict__ src, long long words, int vec)
+{
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (vec) {
+    const long long pairs = words / 2;
+    const double2 *s2 = reinterpret_cast<const double2 *>(src);
+    double2 *d2 = reinterpret_cast<double2 *>(dst);
+    for (long long k = i; k < pairs; k += stride) d2[k] = s2[k];
+    if (i == 0 && (words & 1)) dst[words - 1] = src[words - 1];
+  } else {
+    for (long long k = i; k < words; k += stride) dst[k] = src[k];
+  }
+}
+
+extern "C" int lgb_op_copy_in(double *dst, const double *src, long long words, int nsm, void *stream)
+{
+  if (words <= 0) return 0;
+  const int vec = ((((uintptr_t)dst) | ((uintptr_t)src)) & 15) == 0;
+  const long long items = vec ? words / 2 + 1 : words;
+  const long long need = (items + 255) / 256, cap = 8LL * (nsm > 0 ? nsm : 1);
+  const int grid = (int)(need < cap ? need : cap);
+  k_copy_in<<<grid, 256, 0, (cudaStream_t)stream>>>(dst, src, words, vec);
+  lgb_count_launch(1);
+  return (int)cudaGetLastError();
+}

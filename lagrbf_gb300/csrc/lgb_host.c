@@ -230,7 +230,8 @@ typedef struct {
   int64_t *pid_d, *pid_p;
   int pid_d_cap, pid_p_cap;
   /* direct output: device copy of the particle pids, pid -> swarm index scratch, status flag */
-  int out_direct;        /* option output_direct and the device reads/writes pageable host memory */
+  int out_direct;        /* option output_direct and the device reads/writes pageable host memory:
+                            output rows written and data arrays read by the device directly */
   long long *pidd;
   int pidd_cap, pidd_valid;
   int *out_inv, *out_bad;
@@ -493,16 +494,49 @@ static int create_ctx(lgb_ctx **out)
 /* ---------------------------------------------------------------------------------------- */
 /* swarm filling                                                                            */
 /* ---------------------------------------------------------------------------------------- */
-static int check_box(const lgb_geom *g, int n, const double *x)
+/* DMSwarmAssignRankFromDMDA (swarm_utils.c:854-871) on one rank: every coordinate inside [O, L].
+   One branch-free pass (vectorised) that also compares the words with `prev` when given: *same = 1
+   when all n*dim words are equal.  The first offending point is searched only when one exists. */
+static int check_box(const lgb_geom *g, int n, const double *x, const double *prev, int *same)
 {
-  /* DMSwarmAssignRankFromDMDA (swarm_utils.c:854-871) on one rank */
-  int p, d;
-  for (p = 0; p < n; p++)
-    for (d = 0; d < g->dim; d++) {
-      double v = x[(size_t)p * g->dim + d];
-      if (v < g->O[d] || v > g->L[d])
-        return set_error(LAGRBF_ERR_ARG_WRONG, "point %d does not belong to the PU mesh bounding box", p);
+  const int dim = g->dim;
+  const double lx = g->O[0], hx = g->L[0], ly = g->O[1], hy = g->L[1];
+  const double lz = g->O[dim - 1], hz = g->L[dim - 1];
+  uint64_t diff = 0;
+  int out = 0, p, d;
+  if (dim == 3) {
+    for (p = 0; p < n; p++) {
+      const double a = x[3 * (size_t)p], b = x[3 * (size_t)p + 1], c = x[3 * (size_t)p + 2];
+      out |= (a < lx) | (a > hx) | (b < ly) | (b > hy) | (c < lz) | (c > hz);
     }
+  } else {
+    for (p = 0; p < n; p++) {
+      const double a = x[(size_t)dim * p], b = x[(size_t)dim * p + 1];
+      out |= (a < lx) | (a > hx) | (b < ly) | (b > hy);
+    }
+  }
+  if (out) {
+    for (p = 0; p < n; p++)
+      for (d = 0; d < dim; d++) {
+        double v = x[(size_t)p * dim + d];
+        if (v < g->O[d] || v > g->L[d])
+          return set_error(LAGRBF_ERR_ARG_WRONG, "point %d does not belong to the PU mesh bounding box", p);
+      }
+  }
+  if (same) {
+    *same = 0;
+    if (prev) {
+      const size_t nw = (size_t)n * dim;
+      size_t i;
+      for (i = 0; i < nw; i++) {
+        uint64_t a, b;
+        memcpy(&a, &x[i], sizeof a);
+        memcpy(&b, &prev[i], sizeof b);
+        diff |= a ^ b;
+      }
+      *same = (diff == 0);
+    }
+  }
   return 0;
 }
 
@@ -638,9 +672,7 @@ static int fill_data(lgb_ctx *c, int n, const double *coords, const double *valu
   lgb_dev *d = &c->d;
   int dim = d->g.dim, F = d->F, err = 0, same_coords;
   int old = d->nd;
-  TRY(check_box(&d->g, n, coords));
-  same_coords = (c->hx_d && n == d->nd && n > 0 &&
-                 memcmp(c->hx_d, coords, sizeof(double) * (size_t)n * dim) == 0);
+  TRY(check_box(&d->g, n, coords, (c->hx_d && n == d->nd && n > 0) ? c->hx_d : NULL, &same_coords));
   TRY(grow_pids(&c->pid_d, &c->pid_d_cap, old, n));
   if (pidx) memcpy(c->pid_d, pidx, sizeof(int64_t) * (size_t)n);
   else assign_pids(c->pid_d, old, n);
@@ -660,11 +692,16 @@ static int fill_data(lgb_ctx *c, int n, const double *coords, const double *valu
   }
   if (n > old && F > 0) CU(cudaMemsetAsync(d->fd + (size_t)old * F, 0, sizeof(double) * (size_t)(n - old) * F, c->stream));
   d->nd = n;
-  /* unchanged coordinates (compared word for word above) are already on the device */
-  if (n > 0 && !same_coords)
-    CU(cudaMemcpyAsync(d->xd, coords, sizeof(double) * (size_t)n * dim, cudaMemcpyHostToDevice, c->stream));
-  if (values && n > 0 && F > 0)
-    CU(cudaMemcpyAsync(d->fd, values, sizeof(double) * (size_t)n * F, cudaMemcpyHostToDevice, c->stream));
+  /* unchanged coordinates (compared word for word above) are already on the device; where the
+     device reads pageable host memory it copies the caller's arrays itself */
+  if (n > 0 && !same_coords) {
+    if (c->out_direct) OP(lgb_op_copy_in(d->xd, coords, (long long)n * dim, d->nsm, c->stream));
+    else CU(cudaMemcpyAsync(d->xd, coords, sizeof(double) * (size_t)n * dim, cudaMemcpyHostToDevice, c->stream));
+  }
+  if (values && n > 0 && F > 0) {
+    if (c->out_direct) OP(lgb_op_copy_in(d->fd, values, (long long)n * F, d->nsm, c->stream));
+    else CU(cudaMemcpyAsync(d->fd, values, sizeof(double) * (size_t)n * F, cudaMemcpyHostToDevice, c->stream));
+  }
   if (same_coords) {
     OP(lgb_op_data_values(d, c->stream));
   } else {
@@ -728,7 +765,7 @@ static int fill_points(lgb_ctx *c, int n, const double *coords, const double *va
 {
   lgb_dev *d = &c->d;
   int dim = d->g.dim, F = d->F, err = 0, old = d->np;
-  TRY(check_box(&d->g, n, coords));
+  TRY(check_box(&d->g, n, coords, NULL, NULL));
   TRY(grow_pids(&c->pid_p, &c->pid_p_cap, old, n));
   if (pidx) memcpy(c->pid_p, pidx, sizeof(int64_t) * (size_t)n);
   else assign_pids(c->pid_p, old, n);
