@@ -198,6 +198,7 @@ __global__ void __launch_bounds__(FACT_T) k_factor(FactorParams P)
 {
   __shared__ int s_cstart[8], s_cnt[8], s_off[8];
   __shared__ int s_fail;
+  __shared__ double s_rd;
   __shared__ double s_diag[32 * 33], s_y[4 * 32];
   const lgb_geom &g = P.g;
   const int nwork = P.ctrl->nwork;
@@ -268,18 +269,23 @@ __global__ void __launch_bounds__(FACT_T) k_factor(FactorParams P)
             A[(size_t)j * m + i] = s;
           }
           __syncthreads();
-          double dd = A[(size_t)j * m + j];
-          if (!(dd > 0.0)) {
-            if (tid == 0) {
+          /* one thread takes the pivot's square root and its reciprocal; the column is scaled by
+             multiplication (an FP64 division per entry would cost the FP64 pipe ~10 operations) */
+          if (tid == 0) {
+            const double dd = A[(size_t)j * m + j];
+            if (!(dd > 0.0)) {
               if (atomicCAS(&P.ctrl->factor_error, 0, j + 1) == 0) P.ctrl->factor_node = node;
               s_fail = 1;
+            } else {
+              const double sd = sqrt(dd);
+              A[(size_t)j * m + j] = sd;
+              s_rd = 1.0 / sd;
             }
-            break;
           }
-          dd = sqrt(dd);
-          for (int i = j + 1 + tid; i < m; i += FACT_T) A[(size_t)j * m + i] /= dd;
           __syncthreads();
-          if (tid == 0) A[(size_t)j * m + j] = dd;
+          if (s_fail) break;
+          const double rd = s_rd;
+          for (int i = j + 1 + tid; i < m; i += FACT_T) A[(size_t)j * m + i] *= rd;
           __syncthreads();
         }
         __syncthreads();
