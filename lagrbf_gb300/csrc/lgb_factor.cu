@@ -21,7 +21,7 @@
  */
 #include "lgb_common.cuh"
 
-#define FACT_T 256
+#define FACT_T LGB_FACT_T
 #define CHOL_NB 16 /* columns per Cholesky panel */
 
 struct FactorParams {

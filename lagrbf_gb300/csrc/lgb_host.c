@@ -601,7 +601,7 @@ static int ensure_pools(lgb_ctx *c)
     long long m = d->max_patch > 0 ? d->max_patch : 1;
     long long stride = m * m + m * (d->g.dim + d->F) + m * 17 + 32; /* + Cholesky panel rows */
     long long budget = 4LL << 30;
-    int nws = 4 * d->nsm; /* four patches per SM in flight: the solves are latency bound */
+    int nws = (1024 / LGB_FACT_T) * d->nsm; /* patches in flight per SM: barriers and loads are hidden by the others */
     if ((long long)nws * stride * 8 > budget) nws = (int)(budget / (stride * 8));
     if (nws < 1) nws = 1;
     if (stride != d->ws_stride || nws != d->nws) {

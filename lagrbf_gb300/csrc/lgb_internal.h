@@ -43,6 +43,8 @@ enum { LGB_VF_NONE = 0, LGB_VF_ROTATION = 1, LGB_VF_CELLULAR = 2, LGB_VF_ABC = 3
    holds a coordinate for two particles), then the coefficients of the ninv corner patches that
    contain the point, field-major (field f, patch j at f*ninv + j), each stored LGB_REC32_DUP times,
    padded to a multiple of 16 bytes. */
+/* Threads of a patch set-up / solve CTA; (1024 / LGB_FACT_T) CTAs are kept in flight per SM. */
+#define LGB_FACT_T 128
 #define LGB_REC32_HEAD 8
 #ifndef LGB_REC32_DUP
 #define LGB_REC32_DUP 1

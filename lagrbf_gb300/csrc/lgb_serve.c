@@ -88,8 +88,13 @@ static long long dataset_bytes(const lagrbf_job_t *j)
     nnodes *= j->nodes[d];
   }
   m = 2LL * (1 << j->dim) * ((long long)j->nd / (ncells > 0 ? ncells : 1) + 1) + 16; /* largest patch, generous */
-  return (long long)j->nd * (long long)(400 + 120 * (1 << j->dim) * j->dim) + nnodes * 64 +
-         4LL * 160 * m * m * 8 + (64LL << 20);
+  {
+    /* factorisation workspace: (1024 / LGB_FACT_T) patch slots per SM (160 SMs assumed), at most
+       4 GB, as the context sizes it */
+    long long ws = (1024LL / LGB_FACT_T) * 160 * m * m * 8;
+    if (ws > (4LL << 30)) ws = 4LL << 30;
+    return (long long)j->nd * (long long)(400 + 120 * (1 << j->dim) * j->dim) + nnodes * 64 + ws + (64LL << 20);
+  }
 }
 
 static srv_dataset *find_ds(srv_t *s, int64_t id)
