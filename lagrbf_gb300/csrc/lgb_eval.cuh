@@ -404,11 +404,10 @@ __device__ __forceinline__ void eval_dispatch(int o, const Real *rec, int n, con
 
 /* Node-index range [lo, hi] along one axis that contains every node within the weight support of
    coordinate x. */
-__device__ __forceinline__ void eval_node_range(double x, double O, double h, int n, double rad, int &lo, int &hi)
+__device__ __forceinline__ void eval_node_range(double x, double O, double ih, int n, double rad, int &lo, int &hi)
 {
-  /* nodes i with |x - (O + i h)| < rad; the 1e-6 margin (in node spacings) covers rounding, and a
-     node at distance >= rad has phiW == 0 exactly, so the range is never too small */
-  const double ih = 1.0 / h;
+  /* nodes i with |x - (O + i h)| < rad (ih = 1 / h); the 1e-6 margin (in node spacings) covers
+     rounding, and a node at distance >= rad has phiW == 0 exactly, so the range is never too small */
   int a = (int)ceil((x - rad - O) * ih - 1e-6);
   int b = (int)floor((x + rad - O) * ih + 1e-6);
   lo = (a < 0) ? 0 : a;
@@ -423,11 +422,11 @@ __device__ __forceinline__ void eval_weights(const lgb_geom &g, int ci, int cj, 
                                              const Real *xr, Real (&pw)[EGeo<DIM>::NEN], double &den, int &nsupp)
 {
   constexpr int NEN = EGeo<DIM>::NEN;
-  const double rad = 1.0 / g.eps_w;
+  const double rad = g.rad_w;
   int ilo, ihi, jlo, jhi, klo = 0, khi = 0;
-  eval_node_range(x[0], g.O[0], g.h[0], g.n[0], rad, ilo, ihi);
-  eval_node_range(x[1], g.O[1], g.h[1], g.n[1], rad, jlo, jhi);
-  if constexpr (DIM == 3) eval_node_range(x[2], g.O[2], g.h[2], g.n[2], rad, klo, khi);
+  eval_node_range(x[0], g.O[0], g.rh[0], g.n[0], rad, ilo, ihi);
+  eval_node_range(x[1], g.O[1], g.rh[1], g.n[1], rad, jlo, jhi);
+  if constexpr (DIM == 3) eval_node_range(x[2], g.O[2], g.rh[2], g.n[2], rad, klo, khi);
   nsupp = 0;
   if constexpr (sizeof(Real) == 4) {
     const float epsw = (float)g.eps_w, hf0 = (float)g.h[0], hf1 = (float)g.h[1], hf2 = (float)g.h[2];

@@ -352,6 +352,8 @@ static int read_options(lgb_ctx *c)
   radius = overlap * box / pow((double)g->nnodes, 1.0 / dim); /* partition_of_unity.c:340-344 */
   g->eps_w = 1.0 / radius;
   g->eps_r = shape * g->eps_w;
+  g->rad_w = 1.0 / g->eps_w;
+  for (i = 0; i < 3; i++) g->rh[i] = 1.0 / g->h[i];
   g->wr = 1;
   for (i = 0; i < dim; i++) {
     int w = (int)ceil(radius / g->h[i]);

@@ -59,7 +59,9 @@ typedef struct {
   int nnodes, ncells;
   int wr;          /* weight-support half width in node spacings          */
   double O[3], L[3], h[3];
+  double rh[3];    /* 1 / h, for the fast cell location and the weight-support node range */
   double eps_w, eps_r;
+  double rad_w;    /* 1 / eps_w: the weight support radius as the kernels compute it */
 } lgb_geom;
 
 /* Device-resident control block of the advection loop: the scalars of
@@ -72,7 +74,8 @@ typedef struct {
   double dopri_fac, dopri_fac_min, dopri_fac_max, dopri_atol, dopri_rtol;
   double rmin, rmax;
   double dopri_error;
-  unsigned long long dtcfl_bits;  /* atomicMin target (bits of a positive double)     */
+  unsigned long long n2max_bits;  /* atomicMax target: 1 + bits of the largest |v|^2 of a
+                                     live particle (0: none); the CFL step is computed from it */
   unsigned long long maxerr_bits; /* atomicMax target (bits of a non-negative double) */
   int any_alive;
   int scheme;

@@ -170,11 +170,16 @@ extern "C" int lgb_op_dopri_error(lgb_dev *d, void *stream)
 
 /* velocity <- fields[:, :dim] (when copy), then CFL dt = min cfl*radius/(|v| + 1e-16) and the
    number of live particles. */
+/* AdvectionComputeTimestep_CFL (advection.c:430-470): dt = min_p cfl * r / (|v_p| + 1e-16).  Every
+   step of that expression is a correctly rounded monotone function of |v_p|^2 (sqrt and + rise,
+   the division falls), so the minimum over particles is the expression at the largest |v_p|^2,
+   bit for bit: the kernel only reduces max |v_p|^2 (one FMA chain per particle instead of a square
+   root and a division on the FP64 pipe), and k_ctrl evaluates the expression once. */
 __global__ void k_velocity_cfl(int np, int dim, int F, int copy, const double *__restrict__ fields,
                                double *__restrict__ vel, const int *__restrict__ alive, lgb_ctrl *ctrl)
 {
   int p = blockIdx.x * blockDim.x + threadIdx.x;
-  double dtl = DBL_MAX;
+  unsigned long long nb = 0ull; /* 1 + bits of |v|^2, 0: none (NaN speeds are skipped, as fmin does) */
   int live = 0;
   if (p < np && alive[p]) {
     live = 1;
@@ -184,14 +189,15 @@ __global__ void k_velocity_cfl(int np, int dim, int F, int copy, const double *_
       if (copy) vel[(size_t)p * dim + d] = v;
       n2 += v * v;
     }
-    dtl = ctrl->cfl_fac * ctrl->cfl_radius / (sqrt(n2) + 1e-16);
+    if (n2 == n2) nb = (unsigned long long)__double_as_longlong(n2) + 1ull;
   }
   for (int off = 16; off > 0; off >>= 1) {
-    dtl = fmin(dtl, __shfl_down_sync(0xffffffffu, dtl, off));
+    const unsigned long long o = __shfl_down_sync(0xffffffffu, nb, off);
+    nb = (o > nb) ? o : nb;
     live += __shfl_down_sync(0xffffffffu, live, off);
   }
   if ((threadIdx.x & 31) == 0) {
-    if (dtl < DBL_MAX) atomicMin(&ctrl->dtcfl_bits, (unsigned long long)__double_as_longlong(dtl));
+    if (nb) atomicMax(&ctrl->n2max_bits, nb);
     if (live) atomicAdd(&ctrl->np_alive, live);
   }
 }
@@ -279,11 +285,15 @@ __global__ void k_ctrl(lgb_ctrl *c, int what)
 {
   switch (what) {
   case LGB_CTRL_RESET_CFL:
-    c->dtcfl_bits = (unsigned long long)__double_as_longlong(DBL_MAX);
+    c->n2max_bits = 0ull;
     c->np_alive = 0;
     break;
   case LGB_CTRL_BEGIN_STEP: {
-    double dt_cfl = __longlong_as_double((long long)c->dtcfl_bits);
+    double dt_cfl = DBL_MAX;
+    if (c->n2max_bits) {
+      const double n2 = __longlong_as_double((long long)(c->n2max_bits - 1ull));
+      dt_cfl = c->cfl_fac * c->cfl_radius / (sqrt(n2) + 1e-16);
+    }
     double dt = (c->scheme == LGB_DOPRI) ? ((c->dt_adv < dt_cfl) ? c->dt_adv : dt_cfl) : dt_cfl;
     if (c->t + dt > c->t_next) dt = c->t_next - c->t;
     c->dt = dt;
