@@ -24,14 +24,7 @@ __device__ __forceinline__ int lgb_locate(const lgb_geom &g, const double *x)
     if (d >= g.dim) break;
     double xd = x[d];
     if (!(xd >= g.O[d] && xd <= g.L[d])) return -1;
-    /* floor((x - O) / h) as DMLocatePoints computes it.  a * RN(1/h) differs from RN(a/h) by at
-       most ~3.4e-16 q (three roundings), so both floors agree unless q lies within that distance
-       of an integer; within 1e-15 q + 1e-12 of one the (FP64-pipe heavy) division is taken. */
-    const double a = xd - g.O[d];
-    const double q = a * g.rh[d], tol = 1e-15 * q + 1e-12;
-    double fq = floor(q);
-    if (q - fq < tol || fq + 1.0 - q < tol) fq = floor(a / g.h[d]);
-    int t = (int)fq;
+    int t = (int)floor((xd - g.O[d]) / g.h[d]);
     if (t > g.n[d] - 2) t = g.n[d] - 2;
     if (t < 0) t = 0;
     c[d] = t;

@@ -59,7 +59,7 @@ typedef struct {
   int nnodes, ncells;
   int wr;          /* weight-support half width in node spacings          */
   double O[3], L[3], h[3];
-  double rh[3];    /* 1 / h, for the fast cell location and the weight-support node range */
+  double rh[3];    /* 1 / h, for the weight-support node range */
   double eps_w, eps_r;
   double rad_w;    /* 1 / eps_w: the weight support radius as the kernels compute it */
 } lgb_geom;

@@ -241,7 +241,6 @@ extern "C" LAGRBF_EXPORT int lagrbf_gpu_bin_points_noalloc(int32_t dim, const in
     } else {
       g.n[i] = 1; g.nc[i] = 1; g.O[i] = 0; g.L[i] = 0; g.h[i] = 1.0;
     }
-    g.rh[i] = 1.0 / g.h[i];
     if (ncells > NA_MAX_CELLS) break;
   }
   if (ncells > NA_MAX_CELLS) {
