@@ -4,6 +4,7 @@
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <string.h>
 #include "lgb_internal.h"
 
 #define LGB_CHECK_LAUNCH() do { cudaError_t e__ = cudaGetLastError(); if (e__ != cudaSuccess) return (int)e__; } while (0)
@@ -13,9 +14,21 @@ extern "C" void lgb_count_launch(long long n);
 
 __host__ __device__ static inline int lgb_cdiv(long long a, long long b) { return (int)((a + b - 1) / b); }
 
-/* Cell of a point on the uniform PU mesh; -1 when outside [O, L] (or NaN).  Per axis
-   floor((x - O)/h) in FP64, x == L mapped to the last cell -- the convention the oracle fixes for
-   PETSc's DMLocatePoints on a uniform DMDA. */
+/* Order-preserving integer key of a double: a < b  <=>  key(a) < key(b) for non-NaN values, with
+   -0 and +0 equal; NaNs land beyond +inf or below -inf, i.e. outside any [O, L]. */
+__host__ __device__ __forceinline__ long long lgb_key(double v)
+{
+  long long b;
+  memcpy(&b, &v, sizeof b);
+  if (b == (long long)0x8000000000000000ULL) b = 0;
+  return b >= 0 ? b : (b ^ 0x7fffffffffffffffLL);
+}
+
+/* Cell of a point on the uniform PU mesh (DMSwarmPICSetCellId / DMLocatePoints on a uniform DMDA,
+   the convention the oracle fixes): -1 outside [O, L] or NaN, else per axis
+   clamp(floor((x - O) / h), 0, n - 2) in FP64, x == L in the last cell.  With the face keys the same index is the number
+   of faces at or below x (integer binary search; the FP64 division and floor would keep GB300's
+   FP64 pipe, 1/64 of the FP32 rate, busy for the whole launch). */
 __device__ __forceinline__ int lgb_locate(const lgb_geom &g, const double *x)
 {
   int c[3] = {0, 0, 0};
@@ -23,11 +36,23 @@ __device__ __forceinline__ int lgb_locate(const lgb_geom &g, const double *x)
   for (int d = 0; d < 3; d++) {
     if (d >= g.dim) break;
     double xd = x[d];
-    if (!(xd >= g.O[d] && xd <= g.L[d])) return -1;
-    int t = (int)floor((xd - g.O[d]) / g.h[d]);
-    if (t > g.n[d] - 2) t = g.n[d] - 2;
-    if (t < 0) t = 0;
-    c[d] = t;
+    if (g.bkey) {
+      const long long k = lgb_key(xd);
+      if (k < g.okey[d] || k > g.lkey[d]) return -1;
+      const long long *b = g.bkey + g.boff[d];
+      int lo = 0, hi = g.n[d] - 2; /* faces b[0 .. n-3]; the answer is how many are <= k */
+      while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (__ldg(b + mid) <= k) lo = mid + 1; else hi = mid;
+      }
+      c[d] = lo;
+    } else {
+      if (!(xd >= g.O[d] && xd <= g.L[d])) return -1;
+      int t = (int)floor((xd - g.O[d]) / g.h[d]);
+      if (t > g.n[d] - 2) t = g.n[d] - 2;
+      if (t < 0) t = 0;
+      c[d] = t;
+    }
   }
   return c[0] + c[1] * g.nc[0] + c[2] * g.nc[0] * g.nc[1];
 }

@@ -299,7 +299,7 @@ static void destroy_ctx(lgb_ctx *c)
   DFREE(d->need); DFREE(d->work); DFREE(d->status); DFREE(d->coff); DFREE(d->foff); DFREE(d->c64);
   DFREE(d->c32); DFREE(d->fac); DFREE(d->ws); DFREE(d->pcount); DFREE(d->pstart); DFREE(d->pfill);
   DFREE(d->chunk_start); DFREE(d->scan_tmp); DFREE(d->scan_tmp64); DFREE(d->ctrl);
-  DFREE(d->rec32); DFREE(d->rec_off);
+  DFREE(d->rec32); DFREE(d->rec_off); DFREE(d->bkey_buf);
   for (i = 0; i < 2 * NPROF; i++) if (c->ev[i]) cudaEventDestroy(c->ev[i]);
   if (c->hctrl) cudaFreeHost(c->hctrl);
   if (c->stream) cudaStreamDestroy(c->stream);
@@ -309,6 +309,67 @@ static void destroy_ctx(lgb_ctx *c)
 }
 
 /* LagRBFSetFromOptions + PUSetFromOptions + PUCreateDMDA + ComputeSupport/ShapeFactor */
+/* The device's order-preserving integer key of a double (lgb_key in lgb_common.cuh). */
+static long long face_key(double v)
+{
+  long long b;
+  memcpy(&b, &v, sizeof b);
+  if (b == (long long)0x8000000000000000ULL) b = 0;
+  return b >= 0 ? b : (b ^ 0x7fffffffffffffffLL);
+}
+
+/* Cell faces of the PU mesh as the device's cell location uses them: per axis and k = 1 .. n-2 the
+   smallest coordinate x in [O, L] with floor((x - O) / h) >= k, found from O + k h by stepping one
+   ulp at a time (IEEE subtraction, division and floor give the same result here as on the device).
+   Returns 0 and leaves g->bkey NULL (FP64 division on the device) if a face is not found within a
+   few thousand ulps. */
+static int build_face_keys(lgb_dev *d, cudaStream_t stream)
+{
+  lgb_geom *g = &d->g;
+  int dim = g->dim, total = 0, ax, k, err = 0;
+  long long *hk;
+  for (ax = 0; ax < dim; ax++) total += (g->n[ax] > 2) ? g->n[ax] - 2 : 0;
+  for (ax = 0; ax < 3; ax++) {
+    g->okey[ax] = face_key(g->O[ax]);
+    g->lkey[ax] = face_key(g->L[ax]);
+  }
+  hk = (long long *)malloc(sizeof(long long) * (size_t)(total > 0 ? total : 1));
+  if (!hk) return 0;
+  total = 0;
+  for (ax = 0; ax < dim; ax++) {
+    const double O = g->O[ax], L = g->L[ax], h = g->h[ax];
+    g->boff[ax] = total;
+    for (k = 1; k <= g->n[ax] - 2; k++) {
+      double x = O + (double)k * h;
+      int steps = 0;
+      if (x < O) x = O;
+      if (x > L) x = L;
+      if (floor((x - O) / h) >= (double)k) {
+        while (x > O && steps++ < 4096) {
+          const double xp = nextafter(x, -HUGE_VAL);
+          if (floor((xp - O) / h) >= (double)k) x = xp;
+          else break;
+        }
+      } else {
+        while (x < L && floor((x - O) / h) < (double)k && steps++ < 4096) x = nextafter(x, HUGE_VAL);
+      }
+      if (steps >= 4096 || floor((x - O) / h) < (double)k) { free(hk); return 0; }
+      hk[total++] = face_key(x);
+    }
+  }
+  d->bkey_buf = (long long *)dalloc(sizeof(long long) * (size_t)(total > 0 ? total : 1), &err);
+  if (err) { free(hk); return 0; }
+  if (total > 0 && cudaMemcpyAsync(d->bkey_buf, hk, sizeof(long long) * (size_t)total, cudaMemcpyHostToDevice,
+                                   stream) != cudaSuccess) {
+    free(hk);
+    return 0;
+  }
+  cudaStreamSynchronize(stream);
+  free(hk);
+  g->bkey = d->bkey_buf;
+  return 0;
+}
+
 static int read_options(lgb_ctx *c)
 {
   lgb_dev *d = &c->d;
@@ -462,6 +523,7 @@ static int create_ctx(lgb_ctx **out)
     destroy_ctx(c);
     return set_error(LAGRBF_ERR_SUP, "PU mesh too large (ncells, nnodes <= 8M)");
   }
+  build_face_keys(d, c->stream);
   cudaMemsetAsync(d->setup, 0, sizeof(int) * (size_t)nn, c->stream);
   cudaMemsetAsync(d->solved, 0, sizeof(int) * (size_t)nn, c->stream);
   cudaMemsetAsync(d->need, 0, sizeof(int) * 2 * (size_t)nn, c->stream);

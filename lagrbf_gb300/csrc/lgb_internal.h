@@ -62,6 +62,12 @@ typedef struct {
   double rh[3];    /* 1 / h, for the weight-support node range */
   double eps_w, eps_r;
   double rad_w;    /* 1 / eps_w: the weight support radius as the kernels compute it */
+  /* Cell faces as integer keys (lgb_locate): per axis d, bkey[boff[d] + k - 1] is the key of the
+     smallest coordinate whose cell index floor((x - O) / h) reaches k (k = 1 .. n[d] - 2), okey /
+     lkey the keys of O and L.  Device memory; NULL: locate by the FP64 division. */
+  const long long *bkey;
+  int boff[3];
+  long long okey[3], lkey[3];
 } lgb_geom;
 
 /* Device-resident control block of the advection loop: the scalars of
@@ -124,6 +130,7 @@ typedef struct {
   /* precomputed FP32 record blocks streamed by TMA (NULL: gather staging) */
   float *rec32;
   long long *rec_off;
+  long long *bkey_buf; /* device storage of g.bkey (cell-face keys) */
   long long rec_cap;
   int rec_fp;          /* fields per record (= dim) */
   /* scratch for scans */

@@ -487,3 +487,35 @@ def test_uneven_mixture_matches_oracle(scheme):
     assert relerr(f1, f2) <= TOL64
     if scheme == 3:
         assert abs(c.stats()["dt"] - o.dt()) <= 1e-9 * abs(o.dt())
+
+
+@pytest.mark.parametrize("dim,n,O,L", [(3, 32, 0.0, 1.0), (3, 7, -0.3, 1.7), (2, 13, -2.0, -0.5), (2, 160, 0.0, 1.0)])
+def test_locate_at_cell_faces(dim, n, O, L):
+    """Cell location by integer face keys against the oracle's FP64 floor((x - O) / h): points on
+    every face O + k h and one to three ulps either side, on O and L, and -0.0; bit-exact cell ids
+    for data and particles."""
+    rng = np.random.default_rng(n)
+    h = (L - O) / (n - 1)
+    cand = [O, L, np.nextafter(L, -np.inf)]
+    for k in range(n):
+        x = O + k * h
+        cand.append(x)
+        lo = hi = x
+        for _ in range(3):
+            lo, hi = np.nextafter(lo, -np.inf), np.nextafter(hi, np.inf)
+            cand += [lo, hi]
+    if O == 0.0:
+        cand.append(-0.0)
+    cand = np.array([v for v in cand if O <= v <= L])
+    pts = cand[rng.integers(0, len(cand), (6000, dim))]
+    pts = np.ascontiguousarray(np.concatenate([pts, np.tile(cand[:, None], (1, dim))]))
+    vals = np.ascontiguousarray(np.ones((len(pts), 1)))
+    opts = dict(dim=dim, npartitions=[n] * dim, minCoords=np.full(dim, O), maxCoords=np.full(dim, L),
+                overlap=W.pu_overlap(n), nfields=1, kernel=2)
+    c = gpu_ctx(opts)
+    o = Oracle(**opts)
+    c.fill_data(pts, vals)
+    c.fill_points(pts)
+    assert o.fill(True, pts, vals) == 0 and o.fill(False, pts) == 0
+    assert np.array_equal(c.cellids(True, len(pts)), o.cellids(True, len(pts)))
+    assert np.array_equal(c.cellids(False, len(pts)), o.cellids(False, len(pts)))
