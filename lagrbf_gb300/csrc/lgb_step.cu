@@ -151,11 +151,19 @@ __global__ void k_dopri_error(int np, int dim, const double *__restrict__ xp, co
     }
     E = sqrt(1.0 / dim * e2);
   }
-  /* warp max then one atomic per warp (E >= 0 orders like its bit pattern) */
+  /* block max then one atomic per block (E >= 0 orders like its bit pattern) */
+  __shared__ double s_e[32];
   for (int off = 16; off > 0; off >>= 1) E = fmax(E, __shfl_down_sync(0xffffffffu, E, off));
-  if ((threadIdx.x & 31) == 0 && E >= 0.0) {
-    atomicMax(&ctrl->maxerr_bits, (unsigned long long)__double_as_longlong(E));
-    ctrl->any_alive = 1;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+  if (lane == 0) s_e[warp] = E;
+  __syncthreads();
+  if (warp == 0) {
+    E = (lane < nw) ? s_e[lane] : -1.0;
+    for (int off = 16; off > 0; off >>= 1) E = fmax(E, __shfl_down_sync(0xffffffffu, E, off));
+    if (lane == 0 && E >= 0.0) {
+      atomicMax(&ctrl->maxerr_bits, (unsigned long long)__double_as_longlong(E));
+      ctrl->any_alive = 1;
+    }
   }
 }
 
@@ -191,14 +199,29 @@ __global__ void k_velocity_cfl(int np, int dim, int F, int copy, const double *_
     }
     if (n2 == n2) nb = (unsigned long long)__double_as_longlong(n2) + 1ull;
   }
+  /* block reduction, then one atomic per block: per-warp atomics on these two words serialise */
+  __shared__ unsigned long long s_nb[32];
+  __shared__ int s_live[32];
   for (int off = 16; off > 0; off >>= 1) {
     const unsigned long long o = __shfl_down_sync(0xffffffffu, nb, off);
     nb = (o > nb) ? o : nb;
     live += __shfl_down_sync(0xffffffffu, live, off);
   }
-  if ((threadIdx.x & 31) == 0) {
-    if (nb) atomicMax(&ctrl->n2max_bits, nb);
-    if (live) atomicAdd(&ctrl->np_alive, live);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+  if (lane == 0) { s_nb[warp] = nb; s_live[warp] = live; }
+  __syncthreads();
+  if (warp == 0) {
+    nb = (lane < nw) ? s_nb[lane] : 0ull;
+    live = (lane < nw) ? s_live[lane] : 0;
+    for (int off = 16; off > 0; off >>= 1) {
+      const unsigned long long o = __shfl_down_sync(0xffffffffu, nb, off);
+      nb = (o > nb) ? o : nb;
+      live += __shfl_down_sync(0xffffffffu, live, off);
+    }
+    if (lane == 0) {
+      if (nb) atomicMax(&ctrl->n2max_bits, nb);
+      if (live) atomicAdd(&ctrl->np_alive, live);
+    }
   }
 }
 
