@@ -6,18 +6,20 @@
  * MatCholeskyFactor / KSP preonly+PCCHOLESKY (partition_factor.c:37-55, partition_ksp.c:115-172) and
  * the RHS gather + MatMatSolve (partition_factor.c:57-135).
  *
- * One CTA per queued patch (persistent grid over the work list, so the launch is graph-capturable
- * with a device-side count).  The patch matrix is assembled column-major into a per-CTA workspace
- * slot (lower triangle), factored left-looking one column at a time (every thread owns rows, the
- * reads of a column are coalesced and the pivot row is a broadcast), then the F right-hand sides
- * are solved together.  FP64 throughout: the collocation systems are ill-conditioned.  A
+ * One CTA per queued patch at a time (persistent grid over the work list, (1024 / LGB_FACT_T)
+ * CTAs per SM, so the launch is graph-capturable with a device-side count).  The patch matrix is
+ * assembled column-major into a per-CTA workspace slot (lower triangle), factored in panels of
+ * CHOL_NB columns (left-looking inside a panel, then a tiled update of the trailing triangle), then
+ * the F right-hand sides are solved together.  FP64 throughout: the collocation systems are
+ * ill-conditioned.  A
  * non-positive pivot sets ctrl->factor_error (1-based row) and leaves the patch not set up; no
  * trap, no abort.  The factor is then "prepared" for the solves (reciprocal diagonal and scaled
  * diagonal blocks, below); when factors are kept (A_FACTOR / A_KSP) it is packed (column-major
  * lower, m(m+1)/2) so that new field values only need the two triangular solves, which run the same
  * code on the same values as the first solve.
  *
- * Roofline: FP64 pipe (m^3/3 flops per patch); workspace traffic stays in L2 for m <= ~700.
+ * Roofline: FP64 pipe (m^3/3 flops per patch to factor, 2 F m^2 per solve); GB300 issues 2 DFMA
+ * per clock per SM, so FP64 instructions, not bytes, are what the code counts.
  */
 #include "lgb_common.cuh"
 
