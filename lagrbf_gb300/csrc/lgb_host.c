@@ -318,11 +318,18 @@ static long long face_key(double v)
   return b >= 0 ? b : (b ^ 0x7fffffffffffffffLL);
 }
 
+static double key_double(long long k)
+{
+  double v;
+  if (k < 0) k ^= 0x7fffffffffffffffLL;
+  memcpy(&v, &k, sizeof v);
+  return v;
+}
+
 /* Cell faces of the PU mesh as the device's cell location uses them: per axis and k = 1 .. n-2 the
-   smallest coordinate x in [O, L] with floor((x - O) / h) >= k, found from O + k h by stepping one
-   ulp at a time (IEEE subtraction, division and floor give the same result here as on the device).
-   Returns 0 and leaves g->bkey NULL (FP64 division on the device) if a face is not found within a
-   few thousand ulps. */
+   smallest coordinate x in [O, L] with floor((x - O) / h) >= k.  The predicate is monotone in x,
+   so the face is found by bisection over the integer keys of [O, L] (64 steps at most; IEEE
+   subtraction, division and floor give the same result here as on the device). */
 static int build_face_keys(lgb_dev *d, cudaStream_t stream)
 {
   lgb_geom *g = &d->g;
@@ -337,24 +344,17 @@ static int build_face_keys(lgb_dev *d, cudaStream_t stream)
   if (!hk) return 0;
   total = 0;
   for (ax = 0; ax < dim; ax++) {
-    const double O = g->O[ax], L = g->L[ax], h = g->h[ax];
+    const double O = g->O[ax], h = g->h[ax];
     g->boff[ax] = total;
     for (k = 1; k <= g->n[ax] - 2; k++) {
-      double x = O + (double)k * h;
-      int steps = 0;
-      if (x < O) x = O;
-      if (x > L) x = L;
-      if (floor((x - O) / h) >= (double)k) {
-        while (x > O && steps++ < 4096) {
-          const double xp = nextafter(x, -HUGE_VAL);
-          if (floor((xp - O) / h) >= (double)k) x = xp;
-          else break;
-        }
-      } else {
-        while (x < L && floor((x - O) / h) < (double)k && steps++ < 4096) x = nextafter(x, HUGE_VAL);
+      long long lo = g->okey[ax], hi = g->lkey[ax]; /* predicate false at lo (x = O), true at hi */
+      if (!(floor((key_double(hi) - O) / h) >= (double)k)) { free(hk); return 0; }
+      while ((unsigned long long)hi - (unsigned long long)lo > 1ull) { /* unsigned: no overflow */
+        const long long mid = (long long)((unsigned long long)lo + ((unsigned long long)hi - (unsigned long long)lo) / 2);
+        if (floor((key_double(mid) - O) / h) >= (double)k) hi = mid;
+        else lo = mid;
       }
-      if (steps >= 4096 || floor((x - O) / h) < (double)k) { free(hk); return 0; }
-      hk[total++] = face_key(x);
+      hk[total++] = hi;
     }
   }
   d->bkey_buf = (long long *)dalloc(sizeof(long long) * (size_t)(total > 0 ? total : 1), &err);

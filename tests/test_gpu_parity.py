@@ -489,7 +489,8 @@ def test_uneven_mixture_matches_oracle(scheme):
         assert abs(c.stats()["dt"] - o.dt()) <= 1e-9 * abs(o.dt())
 
 
-@pytest.mark.parametrize("dim,n,O,L", [(3, 32, 0.0, 1.0), (3, 7, -0.3, 1.7), (2, 13, -2.0, -0.5), (2, 160, 0.0, 1.0)])
+@pytest.mark.parametrize("dim,n,O,L", [(3, 32, 0.0, 1.0), (3, 7, -0.3, 1.7), (2, 13, -2.0, -0.5), (2, 160, 0.0, 1.0),
+                                       (3, 9, -1.0, 1.0)])
 def test_locate_at_cell_faces(dim, n, O, L):
     """Cell location by integer face keys against the oracle's FP64 floor((x - O) / h): points on
     every face O + k h and one to three ulps either side, on O and L, and -0.0; bit-exact cell ids
