@@ -437,15 +437,27 @@ def main():
     ctx.reset_stats()
     barrier()
     ts = time.perf_counter()
+    phase = {"fill_swarm": 0.0, "interpolation": 0.0, "output": 0.0, "advect_interpolate": 0.0}
     for k in range(ke):
+        # every call returns after its stream has drained, so the host clock splits the step
+        t0 = time.perf_counter()
         ctx.fill_data(xd, fd_alt[k % 2])
+        t1 = time.perf_counter()
         ctx.interpolate_c()
+        t2 = time.perf_counter()
         ctx.output(coords=xo, fvals=fo, pidx=po)
+        t3 = time.perf_counter()
         ctx.advect_interpolate_c(t, t + DT)
+        t4 = time.perf_counter()
+        phase["fill_swarm"] += t1 - t0
+        phase["interpolation"] += t2 - t1
+        phase["output"] += t3 - t2
+        phase["advect_interpolate"] += t4 - t3
         t += DT
     ctx.synchronize()
     barrier()
     ele = allmax(time.perf_counter() - ts)
+    phase_ms = {kk: 1e3 * v / max(ke, 1) for kk, v in phase.items()}
     e2e = allsum(ctx.stats()["particle_steps"]) / ele
     # ---------------- precision stress (Gaussian, small shape parameter) ----------------
     precision = None
@@ -490,7 +502,8 @@ def main():
                      "fp32_vs_fp64_max_abs_pos_err": pos_err,
                      "err_definition": "per component: max_p|a-b| / max_p|b| and RMS(a-b)/RMS(b), fields after 1 step"},
             "e2e": {"value": e2e, "unit": "particle-steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                    "steps": ke, "path": "fill_swarm(data: same coordinates, compared word for word on the host and not "
+                    "steps": ke, "phase_ms_per_step": phase_ms,
+                    "path": "fill_swarm(data: same coordinates, compared word for word on the host and not "
                                          "sent again; nodal values changing every step) + lagrbf_interpolation "
                                          "(all patch coefficients re-solved) + lagrbf_output + "
                                          "lagrbf_advect_interpolate, host numpy buffers"},
