@@ -864,14 +864,18 @@ static int fill_points(lgb_ctx *c, int n, const double *coords, const double *va
   d->np = n;
   if (n > 0) {
     int i, *ones = (int *)malloc(sizeof(int) * (size_t)n);
+    cudaError_t e = cudaSuccess;
     if (!ones) return set_error(LAGRBF_ERR_MEM, "out of host memory");
     for (i = 0; i < n; i++) ones[i] = 1;
-    CU(cudaMemcpyAsync(d->xp, coords, sizeof(double) * (size_t)n * dim, cudaMemcpyHostToDevice, c->stream));
-    if (values && F > 0)
-      CU(cudaMemcpyAsync(d->fields, values, sizeof(double) * (size_t)n * F, cudaMemcpyHostToDevice, c->stream));
-    CU(cudaMemcpyAsync(d->alive, ones, sizeof(int) * (size_t)n, cudaMemcpyHostToDevice, c->stream));
-    CU(cudaStreamSynchronize(c->stream));
+    e = cudaMemcpyAsync(d->xp, coords, sizeof(double) * (size_t)n * dim, cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess && values && F > 0)
+      e = cudaMemcpyAsync(d->fields, values, sizeof(double) * (size_t)n * F, cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(d->alive, ones, sizeof(int) * (size_t)n, cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
     free(ones);
+    if (e != cudaSuccess)
+      return set_error(LAGRBF_ERR_GPU, "copying the particles to the device failed: %s", cudaGetErrorString(e));
   }
   OP(lgb_op_bin_particles(d, 1, c->stream));
   TRY(choose_chunk(c));
