@@ -60,6 +60,16 @@ int lgb_ctx_dims(void *ctx, int *dim, int *nfields);
       return set_error(e_ == cudaErrorMemoryAllocation ? LAGRBF_ERR_MEM : LAGRBF_ERR_GPU, "%s: %s (%s:%d)", \
                        #call, cudaGetErrorString(e_), __FILE__, __LINE__);                          \
   } while (0)
+/* CU with a cleanup statement (freeing host buffers) run before the error return */
+#define CUF(call, cleanup)                                                                          \
+  do {                                                                                              \
+    cudaError_t e_ = (call);                                                                        \
+    if (e_ != cudaSuccess) {                                                                        \
+      cleanup;                                                                                      \
+      return set_error(e_ == cudaErrorMemoryAllocation ? LAGRBF_ERR_MEM : LAGRBF_ERR_GPU, "%s: %s (%s:%d)", \
+                       #call, cudaGetErrorString(e_), __FILE__, __LINE__);                          \
+    }                                                                                               \
+  } while (0)
 #define OP(call)                                                                                    \
   do {                                                                                              \
     int e_ = (call);                                                                                \
@@ -648,10 +658,10 @@ static int ensure_pools(lgb_ctx *c)
     int *pm = (int *)malloc(sizeof(int) * (size_t)nn), i;
     long long *fo = (long long *)malloc(sizeof(long long) * (size_t)(nn + 1));
     if (!pm || !fo) { free(pm); free(fo); return set_error(LAGRBF_ERR_MEM, "out of host memory"); }
-    CU(cudaMemcpy(pm, d->pm, sizeof(int) * (size_t)nn, cudaMemcpyDeviceToHost));
+    CUF(cudaMemcpy(pm, d->pm, sizeof(int) * (size_t)nn, cudaMemcpyDeviceToHost), (free(pm), free(fo)));
     for (i = 0; i < nn; i++) { fo[i] = ftotal; ftotal += (long long)pm[i] * (pm[i] + 1) / 2; }
     fo[nn] = ftotal;
-    CU(cudaMemcpy(d->foff, fo, sizeof(long long) * (size_t)(nn + 1), cudaMemcpyHostToDevice));
+    CUF(cudaMemcpy(d->foff, fo, sizeof(long long) * (size_t)(nn + 1), cudaMemcpyHostToDevice), (free(pm), free(fo)));
     free(pm); free(fo);
     if (ftotal > d->fac_cap) {
       DFREE(d->fac);
@@ -697,7 +707,7 @@ static int ensure_records(lgb_ctx *c)
   cs = (int *)malloc(sizeof(int) * (size_t)(nc + 1));
   off = (long long *)malloc(sizeof(long long) * (size_t)(nc + 1));
   if (!cs || !off) { free(cs); free(off); return set_error(LAGRBF_ERR_MEM, "out of host memory"); }
-  CU(cudaMemcpy(cs, d->cstart, sizeof(int) * (size_t)(nc + 1), cudaMemcpyDeviceToHost));
+  CUF(cudaMemcpy(cs, d->cstart, sizeof(int) * (size_t)(nc + 1), cudaMemcpyDeviceToHost), (free(cs), free(off)));
   for (cell = 0; cell < nc; cell++) {
     int cxy = g->nc[0] * g->nc[1], l = cell / cxy, r = cell - l * cxy, j = r / g->nc[0], i = r - j * g->nc[0];
     off[cell] = total;
@@ -726,7 +736,7 @@ static int ensure_records(lgb_ctx *c)
     d->rec_cap = err ? 0 : total;
   }
   if (err) { free(off); DFREE(d->rec32); d->rec_cap = 0; return 0; /* fall back to gather staging */ }
-  CU(cudaMemcpy(d->rec_off, off, sizeof(long long) * (size_t)(nc + 1), cudaMemcpyHostToDevice));
+  CUF(cudaMemcpy(d->rec_off, off, sizeof(long long) * (size_t)(nc + 1), cudaMemcpyHostToDevice), free(off));
   free(off);
   return 0;
 }
@@ -796,8 +806,8 @@ static int choose_chunk(lgb_ctx *c)
   double bestcost = -1.0;
   int *cnt = (int *)malloc(sizeof(int) * (size_t)(nc + 1));
   if (!cnt) return set_error(LAGRBF_ERR_MEM, "out of host memory");
-  CU(cudaMemcpyAsync(cnt, d->pstart, sizeof(int) * (size_t)(nc + 1), cudaMemcpyDeviceToHost, c->stream));
-  CU(cudaStreamSynchronize(c->stream));
+  CUF(cudaMemcpyAsync(cnt, d->pstart, sizeof(int) * (size_t)(nc + 1), cudaMemcpyDeviceToHost, c->stream), free(cnt));
+  CUF(cudaStreamSynchronize(c->stream), free(cnt));
   for (m = 4; m >= 1; m--) {
     double cost = 0.0;
     int cap = 64 * m, twarps = 2 * m;
@@ -1437,7 +1447,7 @@ LAGRBF_EXPORT int lagrbf_gpu_get_stats(void *ctx, lagrbf_stats_t *st)
   nn = c->d.g.nnodes;
   setup = (int *)malloc(sizeof(int) * (size_t)nn);
   if (setup) {
-    CU(cudaMemcpy(setup, c->d.setup, sizeof(int) * (size_t)nn, cudaMemcpyDeviceToHost));
+    CUF(cudaMemcpy(setup, c->d.setup, sizeof(int) * (size_t)nn, cudaMemcpyDeviceToHost), free(setup));
     for (i = 0; i < nn; i++) ns += setup[i] != 0;
     free(setup);
   }
@@ -1509,19 +1519,21 @@ LAGRBF_EXPORT int64_t lagrbf_gpu_get_patch_csr(void *ctx, int32_t *patch_start, 
   lgb_ctx *c = (lgb_ctx *)ctx;
   lgb_dev *d;
   int nn, nc, nd, i, s;
-  int *pm, *slot, *cstart, *sorted;
+  int *cstart, *sorted;
   long long total = 0;
+  cudaError_t e;
   if (!c) return -set_error(LAGRBF_ERR_ARG_NULL, "context is NULL");
   d = &c->d;
   nn = d->g.nnodes; nc = d->g.ncells; nd = d->nd;
-  pm = (int *)malloc(sizeof(int) * (size_t)nn);
-  slot = (int *)malloc(sizeof(int) * 8 * (size_t)nn);
   cstart = (int *)malloc(sizeof(int) * (size_t)(nc + 1));
   sorted = (int *)malloc(sizeof(int) * (size_t)(nd > 0 ? nd : 1));
-  cudaMemcpy(pm, d->pm, sizeof(int) * (size_t)nn, cudaMemcpyDeviceToHost);
-  cudaMemcpy(slot, d->slot, sizeof(int) * 8 * (size_t)nn, cudaMemcpyDeviceToHost);
-  cudaMemcpy(cstart, d->cstart, sizeof(int) * (size_t)(nc + 1), cudaMemcpyDeviceToHost);
-  if (nd > 0) cudaMemcpy(sorted, d->sorted, sizeof(int) * (size_t)nd, cudaMemcpyDeviceToHost);
+  if (!cstart || !sorted) { free(cstart); free(sorted); return -set_error(LAGRBF_ERR_MEM, "out of host memory"); }
+  e = cudaMemcpy(cstart, d->cstart, sizeof(int) * (size_t)(nc + 1), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess && nd > 0) e = cudaMemcpy(sorted, d->sorted, sizeof(int) * (size_t)nd, cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) {
+    free(cstart); free(sorted);
+    return -set_error(LAGRBF_ERR_GPU, "copying the cell lists failed: %s", cudaGetErrorString(e));
+  }
   for (i = 0; i < nn; i++) {
     int nxy = d->g.n[0] * d->g.n[1], l = i / nxy, r = i - l * nxy, j = r / d->g.n[0], ii = r - j * d->g.n[0];
     if (patch_start) patch_start[i] = (int)total;
@@ -1536,10 +1548,9 @@ LAGRBF_EXPORT int64_t lagrbf_gpu_get_patch_csr(void *ctx, int32_t *patch_start, 
         total++;
       }
     }
-    (void)pm; (void)slot;
   }
   if (patch_start) patch_start[nn] = (int)total;
-  free(pm); free(slot); free(cstart); free(sorted);
+  free(cstart); free(sorted);
   return total;
 }
 
@@ -1550,13 +1561,19 @@ LAGRBF_EXPORT int64_t lagrbf_gpu_get_block_csr(void *ctx, int32_t *blk_start, in
   int nc, nd, cell;
   int *cstart, *sorted;
   long long total = 0;
+  cudaError_t e;
   if (!c) return -set_error(LAGRBF_ERR_ARG_NULL, "context is NULL");
   d = &c->d;
   nc = d->g.ncells; nd = d->nd;
   cstart = (int *)malloc(sizeof(int) * (size_t)(nc + 1));
   sorted = (int *)malloc(sizeof(int) * (size_t)(nd > 0 ? nd : 1));
-  cudaMemcpy(cstart, d->cstart, sizeof(int) * (size_t)(nc + 1), cudaMemcpyDeviceToHost);
-  if (nd > 0) cudaMemcpy(sorted, d->sorted, sizeof(int) * (size_t)nd, cudaMemcpyDeviceToHost);
+  if (!cstart || !sorted) { free(cstart); free(sorted); return -set_error(LAGRBF_ERR_MEM, "out of host memory"); }
+  e = cudaMemcpy(cstart, d->cstart, sizeof(int) * (size_t)(nc + 1), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess && nd > 0) e = cudaMemcpy(sorted, d->sorted, sizeof(int) * (size_t)nd, cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) {
+    free(cstart); free(sorted);
+    return -set_error(LAGRBF_ERR_GPU, "copying the cell lists failed: %s", cudaGetErrorString(e));
+  }
   for (cell = 0; cell < nc; cell++) {
     int cx = d->g.nc[0], cy = d->g.nc[1], cz = d->g.nc[2];
     int l = cell / (cx * cy), j = (cell - l * cx * cy) / cx, i = cell - l * cx * cy - j * cx, dz, dy, dx;
