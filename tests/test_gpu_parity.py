@@ -520,3 +520,27 @@ def test_locate_at_cell_faces(dim, n, O, L):
     assert o.fill(True, pts, vals) == 0 and o.fill(False, pts) == 0
     assert np.array_equal(c.cellids(True, len(pts)), o.cellids(True, len(pts)))
     assert np.array_equal(c.cellids(False, len(pts)), o.cellids(False, len(pts)))
+
+
+def test_empty_swarms():
+    """No particles, and no data points: the calls succeed, outputs match the oracle (fields of
+    particles with no data in their block stay zero, as the reference leaves them untouched)."""
+    xd, fd, xp, opts = small_3d(np_=300)
+    adv = dict(advection=True, advection_scheme=2, advection_cfl=0.3)
+    c = gpu_ctx(opts, **adv)
+    c.fill_data(xd, fd)
+    c.fill_points(np.empty((0, 3)))
+    c.interpolate_c()
+    c.advect_interpolate_c(0.0, 0.01)
+    assert c.stats()["np_alive"] == 0
+    c2 = gpu_ctx(opts)
+    o = Oracle(**opts)
+    c2.fill_data(np.empty((0, 3)), np.empty((0, 3)))
+    c2.fill_points(xp)
+    c2.interpolate_c()
+    assert o.fill(True, np.empty((0, 3)), np.empty((0, 3))) == 0 and o.fill(False, xp) == 0
+    assert o.interpolate() == 0
+    x1, f1, p1 = gpu_output(c2, len(xp), 3)
+    x2, f2, p2 = o.output(len(xp))
+    assert np.array_equal(p1, p2) and np.array_equal(x1, x2) and np.array_equal(f1, f2)
+    assert not f1.any()
