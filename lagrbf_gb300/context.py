@@ -114,6 +114,10 @@ class LagRBFCtx:
     def store_ref(self, **objs):
         self.refs.update(objs)
 
+    def __index__(self):
+        """The C context pointer (context.py:262-263 of lagrbfpy)."""
+        return self.ctx
+
     def __bool__(self):
         return self.ctx is not None
 
@@ -130,6 +134,10 @@ class LagRBFCtx:
             raise ValueError("Input array cannot be None.\nConsider using an empty array instead: np.empty((0, dim))\n")
         a = np.ascontiguousarray(array, dtype=dtype)
         return a.reshape((a.size,))
+
+    def _end_c(self, array, bs=1):
+        """A flat C array back to rows of bs values (context.py:285-287 of lagrbfpy)."""
+        return array.reshape((-1, bs), order="C")
 
     def _check(self, ierr, name):
         if ierr != 0:

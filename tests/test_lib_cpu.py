@@ -131,3 +131,27 @@ def test_null_context_is_an_error_not_a_crash(lib):
     lib.lagrbf_advect_interpolate.argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.c_double]
     assert lib.lagrbf_advect_interpolate(None, 0.0, 1.0) == 85
     lib.lagrbf_destroy(None)
+
+
+def test_python_surface_mirrors_lagrbfpy():
+    """Every class of lagrbfpy's context, interpolation and advection modules exists in the mirror
+    with every method it defines (inherited ones count); parsed from the LagRBF source tree, skipped
+    without it."""
+    import ast
+    ref = os.path.join(os.environ.get("LAGRBF_REFERENCE", "/root/reference"), "python_api", "lagrbfpy")
+    if not os.path.isdir(ref):
+        pytest.skip("LagRBF source tree not present")
+    deprecated = {"_LagRBFCtx__deprecated_set_advection_function"}  # name-mangled, deprecated in lagrbfpy
+    for rf in ("interface/context.py", "interpolation.py", "advection.py"):
+        with open(os.path.join(ref, rf)) as f:
+            tree = ast.parse(f.read())
+        for cls in [n for n in tree.body if isinstance(n, ast.ClassDef)]:
+            assert hasattr(L, cls.name), cls.name
+            ours = getattr(L, cls.name)
+            for fn in [n for n in cls.body if isinstance(n, ast.FunctionDef)]:
+                name = fn.name
+                if name.startswith("__") and not name.endswith("__"):
+                    name = "_%s%s" % (cls.name, name)
+                if name in deprecated:
+                    continue
+                assert hasattr(ours, name), (cls.name, fn.name)
