@@ -6,10 +6,12 @@ AdvectionInterpolation, AdvectionAnalytical, PointContainer).  PETSc's options d
 replaced by an options store filled from the same keyword arguments.
 """
 from ._lib import load_cfuncs, last_error, Stats  # noqa: F401
-from .points import PointContainer  # noqa: F401
+from .points import PointContainer, fill_datafields  # noqa: F401
 from .context import LagRBFCtx, Options  # noqa: F401
 from .interpolation import LagRBFInterpolator  # noqa: F401
-from .advection import Advection, AdvectionInterpolation, AdvectionAnalytical, FunctionData  # noqa: F401
+from .advection import (Advection, AdvectionInterpolation, AdvectionAnalytical, FunctionData,  # noqa: F401
+                        FunctionPointer)
 
 __all__ = ["LagRBFCtx", "Options", "LagRBFInterpolator", "Advection", "AdvectionInterpolation",
-           "AdvectionAnalytical", "PointContainer", "FunctionData", "load_cfuncs", "last_error", "Stats"]
+           "AdvectionAnalytical", "PointContainer", "FunctionData", "FunctionPointer", "fill_datafields",
+           "load_cfuncs", "last_error", "Stats"]

@@ -6,6 +6,7 @@ import ctypes
 
 import numpy as np
 
+from ._lib import VELOCITY_FN_BATCH
 from .context import LagRBFCtx
 
 
@@ -13,6 +14,26 @@ class FunctionData(ctypes.Structure):
     """Default data structure handed to analytical velocity callbacks
     (lagrbfpy/interface/function_pointer.py)."""
     _fields_ = [("time", ctypes.c_double), ("step", ctypes.c_int32)]
+
+
+class FunctionPointer:
+    """A Python velocity callback and its data as the C function pointer that
+    lagrbf_advection_function_batch takes (lagrbfpy/interface/function_pointer.py:42-120):
+    func(npoints, dim, coords, velocity, data_ptr) -> int; ``cfunc`` is the C pointer, ``data`` the
+    ctypes structure handed to it."""
+
+    def __init__(self, func, data=None):
+        if data is not None and not isinstance(data, ctypes.Structure):
+            raise TypeError("data must be a subclass of ctypes.Structure or FunctionData.\n"
+                            "Build your own class from the helper class FunctionData, e.g.:\n"
+                            "class MyFunctionData(FunctionData):\n"
+                            "    _fields_ = [('param1', ctypes.c_double), ('param2', ctypes.c_int32)]\n")
+        if not callable(func):
+            raise TypeError("func must be a callable function with the signature "
+                            "myfunction(npoints, dim, coords, velocity, data_ptr)\n")
+        self.func = func
+        self.data = data
+        self.cfunc = VELOCITY_FN_BATCH(func)
 
 
 class Advection(LagRBFCtx):

@@ -61,3 +61,52 @@ def test_large_vector_roundtrip(tmp_path):
     a = np.random.default_rng(0).standard_normal((100_003, 3))
     P.write_vec(tmp_path / "big.pbvec", a)
     assert np.array_equal(P.read_vec(tmp_path / "big.pbvec"), a)
+
+
+def test_lagrbfpy_named_vec_functions(tmp_path):
+    """PetscVecWrite / PetscVecLoad (lagrbfpy's names): .info always written, 2D reshaped, files
+    interchangeable with the library's own reader and writer."""
+    a = np.random.default_rng(1).standard_normal((50, 3))
+    f = tmp_path / "v.pbvec"
+    P.PetscVecWrite(f, a)
+    assert (tmp_path / "v.pbvec.info").read_text() == "-vecload_block_size 3\n"
+    assert np.array_equal(P.PetscVecLoad(f), a)
+    assert np.array_equal(P.PetscVecLoadFromFile(f), a.ravel())
+    assert np.array_equal(P.read_vec(f), a)
+    g = tmp_path / "w.pbvec"
+    P.write_vec(g, a)
+    assert np.array_equal(P.PetscVecLoad(g), a)
+    b = np.arange(7.0)
+    P.PetscVecWrite(tmp_path / "b.pbvec", b)
+    assert (tmp_path / "b.pbvec.info").read_text() == "-vecload_block_size 1\n"
+    assert np.array_equal(P.PetscVecLoad(tmp_path / "b.pbvec"), b.reshape(-1, 1))
+    P.PetscVecWriteToFile(tmp_path / "c.pbvec", b)
+    assert np.array_equal(P.PetscVecLoad(tmp_path / "c.pbvec"), b)  # no .info: flat
+    (tmp_path / "bad.info").write_text("-other 3\n")
+    with pytest.raises(ValueError):
+        P.PetscVecLoadBlockSizeFromFile(tmp_path / "bad.info")
+
+
+def test_lagrbfpy_named_is_and_mat_functions(tmp_path):
+    idx = np.array([5, 0, 2**31 - 1, 7])
+    P.PetscISWriteToFile(tmp_path / "i.pbis", idx)
+    r = P.PetscISLoadFromFile(tmp_path / "i.pbis")
+    assert r.dtype == np.int32 and np.array_equal(r, idx)
+    assert np.array_equal(P.read_is(tmp_path / "i.pbis"), idx)
+    with pytest.raises(ValueError):
+        P.PetscISWriteToFile(tmp_path / "j.pbis", [2**31])
+    # AIJ layout: 2 x 3 with entries (0,1)=1.5, (1,0)=-2, (1,2)=4
+    m = tmp_path / "m.pbmat"
+    with open(m, "wb") as fp:
+        np.array([1211216, 2, 3, 3], dtype=">i4").tofile(fp)
+        np.array([1, 2], dtype=">i4").tofile(fp)
+        np.array([1, 0, 2], dtype=">i4").tofile(fp)
+        np.array([1.5, -2.0, 4.0], dtype=">f8").tofile(fp)
+    assert np.array_equal(P.PetscMatDenseLoadFromFile(m), np.array([[0, 1.5, 0], [-2.0, 0, 4.0]]))
+    d = tmp_path / "d.pbmat"
+    with open(d, "wb") as fp:
+        np.array([1211216, 2, 2, -1], dtype=">i4").tofile(fp)
+        np.array([1.0, 2.0, 3.0, 4.0], dtype=">f8").tofile(fp)
+    assert np.array_equal(P.PetscMatDenseLoadFromFile(d), np.array([[1.0, 2.0], [3.0, 4.0]]))
+    with pytest.raises(ValueError):
+        P.PetscMatDenseLoadFromFile(tmp_path / "i.pbis")
