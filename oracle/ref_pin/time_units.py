@@ -7,7 +7,7 @@ Case: 45^3 jittered lattice (91,125 points, ABC flow), 12^3 patches, Wendland C2
   - evaluation: PointwiseInterpolation_AVX512 (interpolation_avx512.c) vs orc_eval,
 for the strict parity build and the fast build of the oracle.
 
-    python oracle/ref_pin/time_units.py
+    LAGRBF_REFERENCE=<LagRBF checkout> python oracle/ref_pin/time_units.py
 """
 import ctypes
 import os

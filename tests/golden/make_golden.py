@@ -1,5 +1,6 @@
 """Generates the golden fixtures of this folder from LagRBF's own hot-loop units (compiled unmodified
-against the PETSc stand-in of oracle/ref_pin/; needs the LagRBF source tree and an AVX-512F host).
+against the PETSc stand-in of oracle/ref_pin/; needs the LagRBF source tree, named by the
+LAGRBF_REFERENCE environment variable, and an AVX-512F host).
 
 Each case stores its seeded inputs and what the reference units return for them:
   weights_ref  SwarmInterpSetWeights_AVX256 (src/swarm/weights_avx.c:97-243), [np, 2^dim]

@@ -15,7 +15,8 @@ from numpy.ctypeslib import ndpointer
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 PIN_DIR = os.path.join(ROOT, "oracle", "ref_pin")
 PIN_SO = os.path.join(ROOT, "oracle", "_ref", "liblagrbf_refpin.so")
-REF = os.environ.get("LAGRBF_REFERENCE", "/root/reference")
+# Location of a LagRBF checkout: required to (re)build the pin, no default.
+REF = os.environ.get("LAGRBF_REFERENCE") or None
 
 _lib = None
 _why = None
@@ -38,10 +39,11 @@ def available():
         return _lib, _why
     if not _has_avx512():
         _why = "host has no AVX-512F"
-    elif not os.path.exists(PIN_SO) and not os.path.isdir(os.path.join(REF, "src")):
-        _why = "LagRBF source tree not present and no prebuilt pin library"
+    elif not os.path.exists(PIN_SO) and not (REF and os.path.isdir(os.path.join(REF, "src"))):
+        _why = ("no prebuilt pin library and no LagRBF source tree (set LAGRBF_REFERENCE to a LagRBF checkout)"
+                if not REF else "LagRBF source tree not found at LAGRBF_REFERENCE=%s" % REF)
     else:
-        if os.path.isdir(os.path.join(REF, "src")):
+        if REF and os.path.isdir(os.path.join(REF, "src")):
             p = subprocess.run(["make", "-s", "-C", PIN_DIR, "REF=" + REF], capture_output=True, text=True)
             if p.returncode != 0:
                 _why = "pin build failed: " + p.stdout[-300:] + p.stderr[-300:]
