@@ -141,6 +141,12 @@ LAGRBF_EXPORT int lagrbf_gpu_set_precision(void *ctx, int fp32);
 /* FP32 FMA throughput of the current device in TFLOP/s, measured by a synthetic kernel
    (dependent FFMA chains, all SMs): the FP32 roofline denominator. */
 LAGRBF_EXPORT double lagrbf_gpu_fp32_peak_tflops(void);
+/* Test hook of the evaluation kernel's bounded waits: poll_limit (> 0) replaces the default number
+   of polls after which a wait on a staging copy gives up (0 restores it); with withhold_copies the
+   kernel arms its staging barriers but issues no copy, so every wait runs out and the call returns
+   LAGRBF_ERR_TIMEOUT with the context still usable.  Applies to the FP32 evaluation of the velocity
+   fields from record blocks (the path of lagrbf_gpu_set_precision(ctx, 1) with F >= dim). */
+LAGRBF_EXPORT int lagrbf_gpu_test_eval_wait(void *ctx, int32_t poll_limit, int32_t withhold_copies);
 /* Kernel-level event timing of the evaluation and factorisation launches (disables graph
    capture while on, so every launch is bracketed by events on the context's stream). */
 LAGRBF_EXPORT int lagrbf_gpu_set_profiling(void *ctx, int on);

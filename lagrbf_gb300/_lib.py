@@ -92,6 +92,7 @@ def register_functions(clib):
     reg("lagrbf_options_get_value", ctypes.c_int, [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_int32])
     # GPU extension
     reg("lagrbf_gpu_set_profiling", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int])
+    reg("lagrbf_gpu_test_eval_wait", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32])
     reg("lagrbf_gpu_advect_resident", ctypes.c_int, [ctypes.c_void_p, PetscReal, PetscReal])
     reg("lagrbf_gpu_set_precision", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int])
     reg("lagrbf_gpu_set_velocity_field", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, real_pn, ctypes.c_int32])

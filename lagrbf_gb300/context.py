@@ -235,6 +235,11 @@ class LagRBFCtx:
     def set_profiling(self, on):
         self._check(self._cf["lagrbf_gpu_set_profiling"](self.ctx, int(bool(on))), "lagrbf_gpu_set_profiling")
 
+    def test_eval_wait(self, poll_limit, withhold_copies=False):
+        """Test hook of the evaluation kernel's bounded waits (lagrbf_gpu_test_eval_wait)."""
+        self._check(self._cf["lagrbf_gpu_test_eval_wait"](self.ctx, int(poll_limit), int(bool(withhold_copies))),
+                    "lagrbf_gpu_test_eval_wait")
+
     def advect_resident(self, time_start, time_end):
         """The advection loop of advect_interpolate_c without its end-of-call reset (data, binning
         and patch set-ups stay resident)."""

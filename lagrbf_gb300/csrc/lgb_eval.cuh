@@ -53,6 +53,8 @@ struct EvalParams {
   int chunk_cap;          /* particles per work unit (blockDim.x * R)     */
   float *rec32;           /* precomputed FP32 record blocks (TMA staging)  */
   const long long *rec_off;
+  int poll_limit;         /* polls of a bounded mbarrier wait before it gives up          */
+  int withhold_copies;    /* test hook: arm the staging barriers but issue no copy         */
 };
 
 enum { KER_GENERIC = 0, KER_C2 = 1, KER_GAUSS = 2 };
@@ -145,6 +147,12 @@ __device__ __forceinline__ f32x2 x2_mul(f32x2 a, f32x2 b)
 {
   f32x2 d;
   asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ f32x2 x2_add(f32x2 a, f32x2 b)
+{
+  f32x2 d;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
   return d;
 }
 __device__ __forceinline__ f32x2 x2_sub(f32x2 a, f32x2 b)

@@ -1,7 +1,7 @@
 /*
  * lgb_eval32_3d.cu -- FP32-evaluation instantiations of the PU evaluation kernel (lgb_eval.cuh), 3D.
  */
-#include "lgb_eval.cuh"
+#include "lgb_evalrec.cuh"
 #include <stdlib.h>
 
 template <int DIM, int FP, int KER, int STAGE, int R>
@@ -27,10 +27,24 @@ static int launch32(const EvalParams &P, int grid, cudaStream_t s)
   return launch32r<DIM, FP, KER, STAGE, 2>(P, grid, s);
 }
 
+/* The record-streamed kernel: EVR_NB stages of P.budget floats, then the PU-weight pairs. */
+template <int DIM, int KER>
+static int launch_rec(const EvalParams &P, int grid, cudaStream_t s)
+{
+  static size_t attr = 0;
+  const size_t smem = (size_t)EVR_NB * P.budget * sizeof(float) + (size_t)(P.chunk_cap / 2) * ((1 << DIM) + 1) * 8;
+  if (smem > attr) {
+    cudaFuncSetAttribute(k_eval_rec<DIM, DIM, KER>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    attr = smem;
+  }
+  k_eval_rec<DIM, DIM, KER><<<grid, P.chunk_cap / 2, smem, s>>>(P);
+  return (int)cudaGetLastError();
+}
+
 template <int DIM, int KER>
 static int launch32_fp(const EvalParams &P, int fp, int stage, int grid, cudaStream_t s)
 {
-  if (stage == 1) return launch32<DIM, DIM, KER, 1>(P, grid, s); /* records hold the dim velocity fields */
+  if (stage == 1) return launch_rec<DIM, KER>(P, grid, s); /* records hold the dim velocity fields */
   switch (fp) {
   case 1: return launch32<DIM, 1, KER, 0>(P, grid, s);
   case 2: return launch32<DIM, 2, KER, 0>(P, grid, s);
@@ -49,6 +63,6 @@ extern "C" int lgb_eval32_launch_3d(const EvalParams *P, int fp, int ker, int st
 
 extern "C" int lgb_build_records_3d(const EvalParams *P, int force, int grid, void *stream)
 {
-  k_build_records<3, 3><<<grid, 128, 0, (cudaStream_t)stream>>>(*P, force);
+  k_build_records2<3, 3><<<grid, 128, 0, (cudaStream_t)stream>>>(*P, force);
   return (int)cudaGetLastError();
 }

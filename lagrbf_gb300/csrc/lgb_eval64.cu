@@ -11,11 +11,12 @@ extern "C" int lgb_eval32_launch_2d(const EvalParams *P, int fp, int ker, int st
 extern "C" int lgb_build_records_3d(const EvalParams *P, int force, int grid, void *stream);
 extern "C" int lgb_build_records_2d(const EvalParams *P, int force, int grid, void *stream);
 
-/* Staging budgets (elements): FP32 gather 30 KB, FP32 TMA 2 x 8 KB (with the running sums: six
-   CTAs per SM; measured best among 4/6/8/12/16 KB rings with the packed FP32 loop), FP64 48 KB. */
+/* Staging budgets (elements): FP32 gather 30 KB, FP32 record stream 4 stages x 4 KB, FP64 48 KB. */
 #define BUDGET32 7680
-#define BUDGET32_TMA 2048
+#define BUDGET32_TMA 1024
 #define BUDGET64 6144
+/* Polls of a bounded mbarrier wait of the evaluation kernel before it reports a timeout. */
+#define EVAL_POLL_LIMIT (1 << 22)
 
 template <int DIM, int FP>
 static int launch64(const EvalParams &P, int grid, cudaStream_t s)
@@ -86,6 +87,8 @@ extern "C" int lgb_op_eval(lgb_dev *d, int nf_first, int nf, double *out, int ou
     P.chunk_cap = d->chunk_cap;
     P.rec32 = d->rec32;
     P.rec_off = d->rec_off;
+    P.poll_limit = d->eval_poll_limit > 0 ? d->eval_poll_limit : EVAL_POLL_LIMIT;
+    P.withhold_copies = d->eval_withhold;
     int rc;
     if (d->prec == LGB_PREC_FP32) {
       const int stage = (d->rec32 && f == 0 && fp == g.dim && d->rec_fp == g.dim) ? 1 : 0;
@@ -112,6 +115,7 @@ extern "C" int lgb_op_build_records(lgb_dev *d, int force, void *stream)
   P.g = d->g;
   P.cstart = d->cstart;
   P.xr32 = d->xr;
+  P.xs64 = d->xs;
   P.c32 = d->c32;
   P.coff = d->coff;
   P.slot = d->slot;

@@ -696,8 +696,8 @@ static int ensure_records(lgb_ctx *c)
 {
   lgb_dev *d = &c->d;
   const lgb_geom *g = &d->g;
-  int nc = g->ncells, cell, o, err = 0;
-  int noff = (g->dim == 3) ? 27 : 9;
+  int nc = g->ncells, cell, vs, err = 0;
+  int nvs = LGB_NVSEG(g->dim);
   int *cs;
   long long *off, total = 0, maxbytes = 16LL << 30;
   const char *env = getenv("LAGRBF_RECORDS_MAX_GB");
@@ -711,13 +711,17 @@ static int ensure_records(lgb_ctx *c)
   for (cell = 0; cell < nc; cell++) {
     int cxy = g->nc[0] * g->nc[1], l = cell / cxy, r = cell - l * cxy, j = r / g->nc[0], i = r - j * g->nc[0];
     off[cell] = total;
-    for (o = 0; o < noff; o++) {
+    for (vs = 0; vs < nvs; vs++) {
+      /* virtual segment vs: neighbour offset o; in 3D the centre cell (o = 13) appears twice, with
+         the coefficients of four corner patches each */
+      int o = (g->dim == 3 && vs > 13) ? vs - 1 : vs;
       int a = o % 3 - 1, b = (o / 3) % 3 - 1, e = (g->dim == 3) ? o / 9 - 1 : 0;
       int ni = i + a, nj = j + b, nl = l + e, nb, ninv, S;
       if (ni < 0 || ni >= g->nc[0] || nj < 0 || nj >= g->nc[1] || nl < 0 || nl >= g->nc[2]) continue;
       nb = ni + nj * g->nc[0] + nl * cxy;
       ninv = (a == 0 ? 2 : 1) * (b == 0 ? 2 : 1) * ((g->dim == 3 && e == 0) ? 2 : 1);
-      S = LGB_REC32_LEN(ninv, g->dim);
+      if (ninv > 4) ninv = 4;
+      S = LGB_REC2_LEN(g->dim, ninv, g->dim);
       total += (long long)(cs[nb + 1] - cs[nb]) * S;
     }
   }
@@ -960,6 +964,18 @@ static int check_factor_error(lgb_ctx *c)
   return 0;
 }
 
+/* A bounded wait of the evaluation kernel that gave up (eval_error in the control block, read into
+   hctrl by the caller): LAGRBF_ERR_TIMEOUT, and the flag is cleared so that the context stays
+   usable for the next call. */
+static int check_eval_error(lgb_ctx *c)
+{
+  if (!c->hctrl->eval_error) return 0;
+  c->hctrl->eval_error = 0;
+  CU(cudaMemsetAsync(&c->d.ctrl->eval_error, 0, sizeof(int), c->stream));
+  CU(cudaStreamSynchronize(c->stream));
+  return set_error(LAGRBF_ERR_TIMEOUT, "a bounded wait of the evaluation kernel gave up");
+}
+
 static int do_interpolation(lgb_ctx *c)
 {
   lgb_dev *d = &c->d;
@@ -969,8 +985,9 @@ static int do_interpolation(lgb_ctx *c)
   TRY(check_factor_error(c));
   if (d->F > 0) TRY(eval_fields(c, 0, d->F, d->fields, d->F));
   prof_collect(c, &c->eval_ms);
+  CU(cudaMemcpyAsync(c->hctrl, c->d.ctrl, sizeof(lgb_ctrl), cudaMemcpyDeviceToHost, c->stream));
   CU(cudaStreamSynchronize(c->stream));
-  return 0;
+  return check_eval_error(c);
 }
 
 static int reset_coefficients(lgb_ctx *c)
@@ -1103,8 +1120,7 @@ static int run_step(lgb_ctx *c, int analytical)
   CU(cudaMemcpyAsync(c->hctrl, c->d.ctrl, sizeof(lgb_ctrl), cudaMemcpyDeviceToHost, c->stream));
   CU(cudaStreamSynchronize(c->stream));
   if (c->hctrl->factor_error) return check_factor_error(c);
-  if (c->hctrl->eval_error) return set_error(LAGRBF_ERR_TIMEOUT, "a bounded wait of the evaluation kernel gave up");
-  return 0;
+  return check_eval_error(c);
 }
 
 static int advection_loop(lgb_ctx *c, double t, double t_next, int analytical, int keep)
@@ -1424,6 +1440,18 @@ LAGRBF_EXPORT int lagrbf_gpu_set_precision(void *ctx, int fp32)
   if (!c) return set_error(LAGRBF_ERR_ARG_NULL, "context is NULL");
   CU(cudaStreamSynchronize(c->stream));
   c->d.prec = fp32 ? LGB_PREC_FP32 : LGB_PREC_FP64;
+  invalidate_graph(c);
+  return 0;
+}
+
+LAGRBF_EXPORT int lagrbf_gpu_test_eval_wait(void *ctx, int32_t poll_limit, int32_t withhold_copies)
+{
+  lgb_ctx *c = (lgb_ctx *)ctx;
+  if (!c) return set_error(LAGRBF_ERR_ARG_NULL, "context is NULL");
+  if (poll_limit < 0) return set_error(LAGRBF_ERR_ARG_OUTOFRANGE, "poll limit must be >= 0");
+  CU(cudaStreamSynchronize(c->stream));
+  c->d.eval_poll_limit = poll_limit;
+  c->d.eval_withhold = withhold_copies ? 1 : 0;
   invalidate_graph(c);
   return 0;
 }

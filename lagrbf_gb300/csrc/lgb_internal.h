@@ -38,13 +38,19 @@ enum { LGB_VF_NONE = 0, LGB_VF_ROTATION = 1, LGB_VF_CELLULAR = 2, LGB_VF_ABC = 3
    (d->chunk_cap, a multiple of 64) is chosen from the particles-per-cell histogram. */
 #define LGB_CHUNK_MAX 256
 
-/* FP32 record of one data point in a cell's precomputed record block: a header {x, x, y, y, z, z,
-   0, 0} (coordinates relative to the evaluating cell's origin, each twice so that one 64-bit pair
-   holds a coordinate for two particles), then the coefficients of the ninv corner patches that
-   contain the point, field-major (field f, patch j at f*ninv + j), each stored LGB_REC32_DUP times,
-   padded to a multiple of 16 bytes. */
+/* FP32 record blocks streamed by the evaluation kernel (lgb_evalrec.cuh): per cell, the data
+   points of its 3^dim neighbour cells in LGB_NVSEG virtual segments (3D: the centre cell twice,
+   with the coefficients of corners 0-3 and of corners 4-7); a record is 2*dim coordinate floats
+   and 2 floats per (field, involved patch), padded to 16 bytes. */
+#define LGB_NVSEG(dim) ((dim) == 3 ? 28 : 9)
+#define LGB_REC2_LEN(dim, ninv, fp) (((2 * (dim) + 2 * (ninv) * (fp) + 3) / 4) * 4)
 /* Threads of a patch set-up / solve CTA; (1024 / LGB_FACT_T) CTAs are kept in flight per SM. */
 #define LGB_FACT_T 128
+/* FP32 record of one data point as the gather kernel stages it in shared memory: a header {x, x, y,
+   y, z, z, 0, 0} (coordinates relative to the evaluating cell's origin, each twice so that one
+   64-bit pair holds a coordinate for two particles), then the coefficients of the ninv corner
+   patches that contain the point, field-major (field f, patch j at f*ninv + j), each stored
+   LGB_REC32_DUP times, padded to a multiple of 16 bytes. */
 #define LGB_REC32_HEAD 8
 #ifndef LGB_REC32_DUP
 #define LGB_REC32_DUP 1
@@ -133,6 +139,8 @@ typedef struct {
   long long *bkey_buf; /* device storage of g.bkey (cell-face keys) */
   long long rec_cap;
   int rec_fp;          /* fields per record (= dim) */
+  int eval_poll_limit; /* polls of the evaluation kernel's bounded waits (0: the default)     */
+  int eval_withhold;   /* test hook: the evaluation kernel arms its staging waits, copies nothing */
   /* scratch for scans */
   int *scan_tmp;
   long long *scan_tmp64;
