@@ -121,6 +121,8 @@ typedef struct {
   double  dt;                 /* the advection context's current time step                   */
   int32_t chunk_cap;          /* particles per evaluation work unit                          */
   int32_t records;            /* 1 when precomputed record blocks are streamed by TMA         */
+  double  kappa_max;          /* largest / median 1-norm condition estimate of the patches     */
+  double  kappa_median;       /* factored with lagrbf_gpu_set_condition_estimates on (else 0)  */
 } lagrbf_stats_t;
 
 /* The interpolated advection loop of lagrbf_advect_interpolate over [time, time_next] without its
@@ -141,6 +143,13 @@ LAGRBF_EXPORT int lagrbf_gpu_set_precision(void *ctx, int fp32);
 /* FP32 FMA throughput of the current device in TFLOP/s, measured by a synthetic kernel
    (dependent FFMA chains, all SMs): the FP32 roofline denominator. */
 LAGRBF_EXPORT double lagrbf_gpu_fp32_peak_tflops(void);
+/* Per-patch condition estimates: while on, every patch factorisation also estimates
+   kappa_1(A) = ||A||_1 ||A^-1||_1 of its collocation matrix (||A^-1||_1 by Hager's method as refined
+   by Higham, a few extra triangular solves per patch; the factorisation itself is unchanged).
+   lagrbf_gpu_get_condition copies the estimates by node (kappa, nullable, nnodes entries, 0 for
+   patches not factored while on) and summary[3] = {max, median, count} of the non-zero ones. */
+LAGRBF_EXPORT int lagrbf_gpu_set_condition_estimates(void *ctx, int on);
+LAGRBF_EXPORT int lagrbf_gpu_get_condition(void *ctx, double *kappa, double *summary);
 /* Test hook of the evaluation kernel's bounded waits: poll_limit (> 0) replaces the default number
    of polls after which a wait on a staging copy gives up (0 restores it); with withhold_copies the
    kernel arms its staging barriers but issues no copy, so every wait runs out and the call returns

@@ -45,7 +45,8 @@ class Stats(ctypes.Structure):
         ("steps", ctypes.c_int64), ("patches_factored", ctypes.c_int64), ("factor_ms", ctypes.c_double),
         ("factor_flops", ctypes.c_double), ("np_alive", ctypes.c_int32), ("nd", ctypes.c_int32),
         ("max_patch", ctypes.c_int32), ("npatch_setup", ctypes.c_int32), ("dt", ctypes.c_double),
-        ("chunk_cap", ctypes.c_int32), ("records", ctypes.c_int32),
+        ("chunk_cap", ctypes.c_int32), ("records", ctypes.c_int32), ("kappa_max", ctypes.c_double),
+        ("kappa_median", ctypes.c_double),
     ]
 
     def as_dict(self):
@@ -92,6 +93,8 @@ def register_functions(clib):
     reg("lagrbf_options_get_value", ctypes.c_int, [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_int32])
     # GPU extension
     reg("lagrbf_gpu_set_profiling", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int])
+    reg("lagrbf_gpu_set_condition_estimates", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int])
+    reg("lagrbf_gpu_get_condition", ctypes.c_int, [ctypes.c_void_p, real_pn, real_pn])
     reg("lagrbf_gpu_test_eval_wait", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32])
     reg("lagrbf_gpu_advect_resident", ctypes.c_int, [ctypes.c_void_p, PetscReal, PetscReal])
     reg("lagrbf_gpu_set_precision", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int])

@@ -235,6 +235,19 @@ class LagRBFCtx:
     def set_profiling(self, on):
         self._check(self._cf["lagrbf_gpu_set_profiling"](self.ctx, int(bool(on))), "lagrbf_gpu_set_profiling")
 
+    def set_condition_estimates(self, on):
+        """Per-patch 1-norm condition estimates at every factorisation (lagrbf_gpu_set_condition_estimates)."""
+        self._check(self._cf["lagrbf_gpu_set_condition_estimates"](self.ctx, int(bool(on))),
+                    "lagrbf_gpu_set_condition_estimates")
+
+    def condition(self):
+        """(kappa by patch node, {"max", "median", "count"}) of the estimates made so far."""
+        ints, _ = self.geometry()
+        k = np.zeros(int(ints[4]))
+        sm = np.zeros(3)
+        self._check(self._cf["lagrbf_gpu_get_condition"](self.ctx, k, sm), "lagrbf_gpu_get_condition")
+        return k, {"max": float(sm[0]), "median": float(sm[1]), "count": int(sm[2])}
+
     def test_eval_wait(self, poll_limit, withhold_copies=False):
         """Test hook of the evaluation kernel's bounded waits (lagrbf_gpu_test_eval_wait)."""
         self._check(self._cf["lagrbf_gpu_test_eval_wait"](self.ctx, int(poll_limit), int(bool(withhold_copies))),

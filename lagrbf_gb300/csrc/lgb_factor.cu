@@ -38,6 +38,7 @@ struct FactorParams {
   float *c32;
   long long ws_stride;
   lgb_ctrl *ctrl;
+  double *kappa;   /* non-NULL: 1-norm condition estimate of every factored patch, by node */
 };
 
 
@@ -196,12 +197,102 @@ __device__ void chol_solve(const double *L, int m, int F, double *B, double *D, 
   }
 }
 
+/* ---- block reductions (FACT_T threads; red: 32 doubles of shared memory) ---- */
+__device__ double blk_reduce(double v, double *red, bool is_max)
+{
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int o = 16; o > 0; o >>= 1) {
+    const double u = __shfl_xor_sync(0xffffffffu, v, o);
+    v = is_max ? fmax(v, u) : v + u;
+  }
+  __syncthreads();
+  if (lane == 0) red[warp] = v;
+  __syncthreads();
+  double r = red[0];
+  for (int w = 1; w < nw; w++) r = is_max ? fmax(r, red[w]) : r + red[w];
+  return r;
+}
+/* Largest |z_i| and its first index. */
+__device__ double blk_argmax_abs(const double *z, int m, int *idx, double *red, int *ired)
+{
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  double best = -1.0;
+  int bi = 0;
+  for (int i = threadIdx.x; i < m; i += blockDim.x)
+    if (fabs(z[i]) > best) { best = fabs(z[i]); bi = i; }
+  for (int o = 16; o > 0; o >>= 1) {
+    const double u = __shfl_xor_sync(0xffffffffu, best, o);
+    const int ui = __shfl_xor_sync(0xffffffffu, bi, o);
+    if (u > best || (u == best && ui < bi)) { best = u; bi = ui; }
+  }
+  __syncthreads();
+  if (lane == 0) { red[warp] = best; ired[warp] = bi; }
+  __syncthreads();
+  best = red[0];
+  bi = ired[0];
+  for (int w = 1; w < nw; w++)
+    if (red[w] > best || (red[w] == best && ired[w] < bi)) { best = red[w]; bi = ired[w]; }
+  *idx = bi;
+  return best;
+}
+
+/* ||A^-1||_1 estimate from the prepared factor in the workspace (Hager's method as refined by Higham:
+   N. J. Higham, "FORTRAN codes for estimating the one-norm of a real or complex matrix", ACM TOMS 14
+   (1988); A symmetric, so A^-T = A^-1): at most five iterations of x -> sign(A^-1 x) -> e_j, then
+   the alternating test vector x_i = (-1)^i (1 + i/(m-1)).  v, u: two workspace vectors of m. */
+__device__ double inv_norm1_estimate(const double *L, int m, double *v, double *u, double *D, double *Y, double *red,
+                                     int *ired)
+{
+  const int tid = threadIdx.x;
+  for (int i = tid; i < m; i += FACT_T) v[i] = 1.0 / m;
+  __syncthreads();
+  chol_solve_group<false, 1>(L, m, v, D, Y);
+  double s = 0.0;
+  for (int i = tid; i < m; i += FACT_T) s += fabs(v[i]);
+  double est = blk_reduce(s, red, false);
+  int jprev = -1;
+  for (int it = 0; it < 5; it++) {
+    for (int i = tid; i < m; i += FACT_T) u[i] = (v[i] >= 0.0) ? 1.0 : -1.0;
+    __syncthreads();
+    chol_solve_group<false, 1>(L, m, u, D, Y);
+    int j;
+    const double zmax = blk_argmax_abs(u, m, &j, red, ired);
+    double ztx;
+    if (jprev < 0) {
+      double t = 0.0;
+      for (int i = tid; i < m; i += FACT_T) t += u[i];
+      ztx = blk_reduce(t, red, false) / m;
+    } else {
+      ztx = u[jprev];
+    }
+    if (it > 0 && zmax <= ztx) break;
+    for (int i = tid; i < m; i += FACT_T) v[i] = (i == j) ? 1.0 : 0.0;
+    __syncthreads();
+    chol_solve_group<false, 1>(L, m, v, D, Y);
+    s = 0.0;
+    for (int i = tid; i < m; i += FACT_T) s += fabs(v[i]);
+    const double e2 = blk_reduce(s, red, false);
+    if (e2 <= est) break;
+    est = e2;
+    jprev = j;
+  }
+  for (int i = tid; i < m; i += FACT_T) v[i] = ((i & 1) ? -1.0 : 1.0) * (1.0 + (m > 1 ? (double)i / (m - 1) : 0.0));
+  __syncthreads();
+  chol_solve_group<false, 1>(L, m, v, D, Y);
+  s = 0.0;
+  for (int i = tid; i < m; i += FACT_T) s += fabs(v[i]);
+  const double alt = 2.0 * blk_reduce(s, red, false) / (3.0 * m);
+  return fmax(est, alt);
+}
+
 __global__ void __launch_bounds__(FACT_T) k_factor(FactorParams P)
 {
   __shared__ int s_cstart[8], s_cnt[8], s_off[8];
   __shared__ int s_fail;
   __shared__ double s_rd;
   __shared__ double s_diag[32 * 33], s_y[4 * 32];
+  __shared__ double s_red[32];
+  __shared__ int s_ired[32];
   const lgb_geom &g = P.g;
   const int nwork = P.ctrl->nwork;
   const int tid = threadIdx.x;
@@ -254,6 +345,18 @@ __global__ void __launch_bounds__(FACT_T) k_factor(FactorParams P)
         }
       }
       __syncthreads();
+      /* 1-norm of the symmetric matrix (largest column sum of |A|) for the condition estimate */
+      double anorm = 0.0;
+      if (P.kappa) {
+        double cm = 0.0;
+        for (int j = tid; j < m; j += FACT_T) {
+          double cs = 0.0;
+          for (int i = j; i < m; i++) cs += fabs(A[(size_t)j * m + i]);
+          for (int k = 0; k < j; k++) cs += fabs(A[(size_t)k * m + j]);
+          cm = fmax(cm, cs);
+        }
+        anorm = blk_reduce(cm, s_red, true);
+      }
       /* Cholesky in panels of CHOL_NB columns: each panel is factored left-looking from the
          entries already updated by the earlier panels, then the trailing lower triangle is updated
          by the panel (tiles of 32 x 32, one warp per tile).  Every entry receives its updates
@@ -323,6 +426,10 @@ __global__ void __launch_bounds__(FACT_T) k_factor(FactorParams P)
       __syncthreads();
       if (s_fail) { __syncthreads(); continue; }
       prepare_diag_blocks<false>(A, m);
+      if (P.kappa) {
+        const double inv = inv_norm1_estimate(A, m, Ps, Ps + m, s_diag, s_y, s_red, s_ired);
+        if (tid == 0) P.kappa[node] = anorm * inv;
+      }
       if (P.keep) {
         double *Fk = P.fac + P.foff[node];
         for (int j = 0; j < m; j++) {
@@ -382,6 +489,7 @@ extern "C" int lgb_op_factor(lgb_dev *d, void *stream)
   P.ws = d->ws;
   P.ws_stride = d->ws_stride;
   P.ctrl = d->ctrl;
+  P.kappa = d->cond_on ? d->kappa : NULL;
   k_factor<<<d->nws, FACT_T, 0, (cudaStream_t)stream>>>(P);
   lgb_count_launch(1);
   return (int)cudaGetLastError();

@@ -306,7 +306,7 @@ static void destroy_ctx(lgb_ctx *c)
   free_data(d);
   free_particles(d);
   DFREE(d->cstart); DFREE(d->dfill); DFREE(d->pm); DFREE(d->slot); DFREE(d->setup); DFREE(d->solved);
-  DFREE(d->need); DFREE(d->work); DFREE(d->status); DFREE(d->coff); DFREE(d->foff); DFREE(d->c64);
+  DFREE(d->need); DFREE(d->work); DFREE(d->status); DFREE(d->coff); DFREE(d->foff); DFREE(d->c64); DFREE(d->kappa);
   DFREE(d->c32); DFREE(d->fac); DFREE(d->ws); DFREE(d->pcount); DFREE(d->pstart); DFREE(d->pfill);
   DFREE(d->chunk_start); DFREE(d->scan_tmp); DFREE(d->scan_tmp64); DFREE(d->ctrl);
   DFREE(d->rec32); DFREE(d->rec_off); DFREE(d->bkey_buf);
@@ -1465,6 +1465,57 @@ LAGRBF_EXPORT int lagrbf_gpu_set_profiling(void *ctx, int on)
   return 0;
 }
 
+static int cmp_double(const void *a, const void *b)
+{
+  const double x = *(const double *)a, y = *(const double *)b;
+  return (x > y) - (x < y);
+}
+
+LAGRBF_EXPORT int lagrbf_gpu_set_condition_estimates(void *ctx, int on)
+{
+  lgb_ctx *c = (lgb_ctx *)ctx;
+  lgb_dev *d;
+  int err = 0;
+  if (!c) return set_error(LAGRBF_ERR_ARG_NULL, "context is NULL");
+  d = &c->d;
+  CU(cudaStreamSynchronize(c->stream));
+  if (on && !d->kappa) {
+    d->kappa = (double *)dalloc(sizeof(double) * (size_t)d->g.nnodes, &err);
+    if (err) return set_error(LAGRBF_ERR_MEM, "condition estimate array allocation failed");
+    CU(cudaMemset(d->kappa, 0, sizeof(double) * (size_t)d->g.nnodes));
+  }
+  d->cond_on = on ? 1 : 0;
+  invalidate_graph(c);
+  return 0;
+}
+
+/* Condition estimates of the patches factored since they were switched on (0 where none). */
+LAGRBF_EXPORT int lagrbf_gpu_get_condition(void *ctx, double *kappa, double *summary)
+{
+  lgb_ctx *c = (lgb_ctx *)ctx;
+  int nn, i, n = 0;
+  double *k;
+  if (!c) return set_error(LAGRBF_ERR_ARG_NULL, "context is NULL");
+  if (summary) summary[0] = summary[1] = summary[2] = 0.0;
+  if (!c->d.kappa) return 0;
+  nn = c->d.g.nnodes;
+  k = (double *)malloc(sizeof(double) * (size_t)nn);
+  if (!k) return set_error(LAGRBF_ERR_MEM, "out of host memory");
+  CU(cudaStreamSynchronize(c->stream));
+  CUF(cudaMemcpy(k, c->d.kappa, sizeof(double) * (size_t)nn, cudaMemcpyDeviceToHost), free(k));
+  if (kappa) memcpy(kappa, k, sizeof(double) * (size_t)nn);
+  for (i = 0; i < nn; i++)
+    if (k[i] > 0.0) k[n++] = k[i];
+  if (summary && n > 0) {
+    qsort(k, (size_t)n, sizeof(double), cmp_double);
+    summary[0] = k[n - 1];
+    summary[1] = (n & 1) ? k[n / 2] : 0.5 * (k[n / 2 - 1] + k[n / 2]);
+    summary[2] = n;
+  }
+  free(k);
+  return 0;
+}
+
 LAGRBF_EXPORT int lagrbf_gpu_get_stats(void *ctx, lagrbf_stats_t *st)
 {
   lgb_ctx *c = (lgb_ctx *)ctx;
@@ -1497,6 +1548,12 @@ LAGRBF_EXPORT int lagrbf_gpu_get_stats(void *ctx, lagrbf_stats_t *st)
   st->dt = c->hctrl->dt_adv;
   st->chunk_cap = c->d.chunk_cap;
   st->records = c->d.rec32 != NULL;
+  if (c->d.cond_on) {
+    double sm[3];
+    TRY(lagrbf_gpu_get_condition(ctx, NULL, sm));
+    st->kappa_max = sm[0];
+    st->kappa_median = sm[1];
+  }
   return 0;
 }
 

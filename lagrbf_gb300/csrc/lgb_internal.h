@@ -125,6 +125,8 @@ typedef struct {
   float *c32;
   int max_patch;
   double *ws;          /* factorisation workspace: nws slots of ws_stride doubles */
+  double *kappa;       /* per-patch 1-norm condition estimates (nnodes), when cond_on    */
+  int cond_on;
   long long ws_stride;
   int nws;
   /* particle swarm */
