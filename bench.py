@@ -232,30 +232,80 @@ def run_uneven(rk4_steps=3, dopri_steps=5):
     return out
 
 
-def run_precision_stress(np_=1_000_000):
-    """The precision-stress configuration at 1M particles: 80^3 jittered lattice, Gaussian kernel
-    with eps_r = 1/h (h the lattice spacing), 16 seeded Fourier modes with amplitudes ~N(0,1)/k^2,
-    32^3 PU nodes; FP32 evaluation against the all-FP64 path on the same factors' data, max and RMS
-    relative error per component, plus the FP64 interpolant against the exact field."""
+def run_precision_stress(np_=1_000_000, eps_h=1.0):
+    """The precision-stress configuration: 80^3 jittered lattice, Gaussian kernel with eps_r = eps_h/h
+    (h the lattice spacing; eps_h = 1 is the configuration as stated), 16 seeded Fourier modes with
+    amplitudes ~N(0,1)/k^2, 32^3 PU nodes; FP32 evaluation against the all-FP64 path on the same
+    data, max / RMS / pointwise relative error per component, the patches' 1-norm condition
+    estimates beside them, plus the FP64 interpolant against the exact field."""
     import lagrbf_gb300 as L
     from lagrbf_gb300 import workloads as W
     xd, fd, xp, opts = W.config_precision_3d(np_=np_)
-    res = {}
+    opts = dict(opts, shape_factor=opts["shape_factor"] * eps_h)
+    res, kap = {}, None
     for prec in ("fp64", "fp32"):
         c = L.LagRBFCtx(**opts, solve_method=1, eval_precision=prec)
+        if prec == "fp64":
+            c.set_condition_estimates(True)
         c.fill_data(xd, fd)
         c.fill_points(xp)
         c.interpolate_c()
         f = np.zeros((np_, 3))
         c.output(fvals=f)
         res[prec] = f
+        if prec == "fp64":
+            kap = c.condition()[1]
         del c
     mx, rms = relerr_stats(res["fp32"], res["fp64"])
     exact = W.fourier_field(xp, np.random.default_rng(7))
     ex_mx, ex_rms = relerr_stats(res["fp64"], exact)
-    return {"workload": "80^3 jittered lattice, Gaussian eps_r = 1/h, 16 Fourier modes, 32^3 PU, %d particles" % np_,
+    return {"workload": "80^3 jittered lattice, Gaussian eps_r = %g/h, 16 Fourier modes, 32^3 PU, %d particles"
+                        % (eps_h, np_),
+            "kappa1_max": kap["max"], "kappa1_median": kap["median"], "patches": kap["count"],
             "fp32_vs_fp64_max_rel_err": mx, "fp32_vs_fp64_rms_rel_err": rms,
+            "fp32_vs_fp64_pointwise_rel_err": pointwise_relerr(res["fp32"], res["fp64"]),
             "fp64_vs_exact_max_rel_err": ex_mx, "fp64_vs_exact_rms_rel_err": ex_rms}
+
+
+def run_trajectory(xd, fd, xp, opts, nsteps=50):
+    """FP32-evaluation vs plain FP64 trajectories: the same particles advanced nsteps RK4 steps
+    (dt = 5e-4) by each path from the same start; position differences against the distance
+    travelled, and the velocity (field) difference at the end."""
+    import lagrbf_gb300 as L
+    n = len(xp)
+    pid = np.arange(1, n + 1, dtype=np.int64)
+    c = L.LagRBFCtx(**opts, advection=True, advection_scheme=2, advection_cfl=0.3, dt=DT, solve_method=1,
+                    eval_precision="fp32")
+    c.fill_data(xd, fd)
+    out = {}
+    for prec in ("fp32", "fp64"):
+        c.set_precision(prec == "fp32")
+        c.fill_points(xp, pidx=pid)
+        c.interpolate_c()
+        t = 0.0
+        for _ in range(nsteps):
+            c.advect_resident(t, t + DT)
+            t += DT
+        x = np.zeros((n, 3)); f = np.zeros((n, 3)); p = np.zeros(n, dtype=np.int64)
+        c.output(coords=x, fvals=f, pidx=p)
+        out[prec] = (x, f, p)
+    (x32, f32, p32), (x64, f64, p64) = out["fp32"], out["fp64"]
+    alive = (p32 > 0) & (p64 > 0)
+    dx = np.abs(x32[alive] - x64[alive])
+    travel = np.linalg.norm(x64[alive] - xp[alive], axis=1)
+    fmx, frms = relerr_stats(f32[alive], f64[alive])
+    return {"particles": n, "steps": nsteps, "alive_both": int(alive.sum()), "same_alive": bool((p32 == p64).all()),
+            "pos_max_abs_diff": float(dx.max()), "pos_rms_abs_diff": float(np.sqrt((dx ** 2).mean())),
+            "pos_max_diff_rel_to_max_travel": float(dx.max() / travel.max()),
+            "vel_max_rel_err": fmx, "vel_rms_rel_err": frms,
+            "vel_pointwise_rel_err": pointwise_relerr(f32[alive], f64[alive])}
+
+
+def pointwise_relerr(a, b, floor=1e-3):
+    """max_p |a - b| / max(|b|, floor * max|b|), per component (floor keeps zeros of b finite)."""
+    den = np.maximum(np.abs(b), floor * np.abs(b).max(axis=0))
+    den[den == 0] = 1.0
+    return [float(x) for x in (np.abs(a - b) / den).max(axis=0)]
 
 
 def relerr_stats(a, b):
@@ -408,6 +458,7 @@ def main():
     ctx.advect_resident(t, t + DT)
     x32, f32, _ = snapshot()
     err_max, err_rms = relerr_stats(f32, f64)
+    err_pw = pointwise_relerr(f32, f64)
     pos_err = float(np.abs(x32 - x64).max())
     # ---------------- plain FP64 path throughput ----------------
     ctx.set_precision(False)
@@ -459,10 +510,15 @@ def main():
     ele = allmax(time.perf_counter() - ts)
     phase_ms = {kk: 1e3 * v / max(ke, 1) for kk, v in phase.items()}
     e2e = allsum(ctx.stats()["particle_steps"]) / ele
+    # ---------------- FP32 vs FP64 trajectories over 50 steps (1M-particle sample) ----------------
+    trajectory = None
+    if rank == 0 and world == 1 and args.serve_jobs > 0:
+        trajectory = run_trajectory(xd, fd, xp[:1 << 20], opts)
     # ---------------- precision stress (Gaussian, small shape parameter) ----------------
     precision = None
     if rank == 0 and world == 1 and args.serve_jobs > 0:
         precision = run_precision_stress()
+        precision["flattened"] = run_precision_stress(np_=250_000, eps_h=0.35)
     # ---------------- serving loop: Poisson stream of mixed advection jobs ----------------
     uneven = None
     if rank == 0 and world == 1 and args.uneven:
@@ -499,8 +555,10 @@ def main():
             "fp64": {"value": value64, "unit": "particle-steps/s", "steps": args.fp64_steps,
                      "fp32_speedup": value / value64 if value64 > 0 else None,
                      "fp32_vs_fp64_max_rel_err": err_max, "fp32_vs_fp64_rms_rel_err": err_rms,
-                     "fp32_vs_fp64_max_abs_pos_err": pos_err,
-                     "err_definition": "per component: max_p|a-b| / max_p|b| and RMS(a-b)/RMS(b), fields after 1 step"},
+                     "fp32_vs_fp64_pointwise_rel_err": err_pw, "fp32_vs_fp64_max_abs_pos_err": pos_err,
+                     "trajectory_50_steps": trajectory,
+                     "err_definition": "per component: max_p|a-b| / max_p|b|, RMS(a-b)/RMS(b), and pointwise "
+                                       "max_p |a-b| / max(|b|, 1e-3 max|b|); fields after 1 step"},
             "e2e": {"value": e2e, "unit": "particle-steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "steps": ke, "phase_ms_per_step": phase_ms,
                     "path": "fill_swarm(data: same coordinates, compared word for word on the host and not "
