@@ -36,7 +36,8 @@ extern "C" int lgb_device_info(int *nsm, int *smem_optin)
 /* locate + histogram                                                                           */
 /* ------------------------------------------------------------------------------------------- */
 __global__ void k_locate(lgb_geom g, int n, const double *__restrict__ x, int *__restrict__ cell,
-                         int *__restrict__ alive, int *__restrict__ counts, int *__restrict__ nbad)
+                         int *__restrict__ alive, int *__restrict__ counts, int *__restrict__ nbad,
+                         const int *__restrict__ active)
 {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
@@ -48,14 +49,14 @@ __global__ void k_locate(lgb_geom g, int n, const double *__restrict__ x, int *_
     if (nbad) atomicAdd(nbad, 1);
     return;
   }
-  if (counts) atomicAdd(&counts[c], 1);
+  if (counts && (!active || active[i])) atomicAdd(&counts[c], 1);
 }
 
 extern "C" int lgb_op_locate(const lgb_geom *g, int n, const double *x, int *cell, int *alive, int *counts,
                              int *nbad, void *stream)
 {
   if (n <= 0) return 0;
-  k_locate<<<lgb_cdiv(n, 256), 256, 0, (cudaStream_t)stream>>>(*g, n, x, cell, alive, counts, nbad);
+  k_locate<<<lgb_cdiv(n, 256), 256, 0, (cudaStream_t)stream>>>(*g, n, x, cell, alive, counts, nbad, NULL);
   lgb_count_launch(1);
   LGB_CHECK_LAUNCH();
   return 0;
@@ -151,11 +152,13 @@ extern "C" int lgb_op_scan_i64(int n, const long long *in, long long *out, long 
 /* scatter into per-cell lists                                                                  */
 /* ------------------------------------------------------------------------------------------- */
 __global__ void k_scatter(int n, const int *__restrict__ cell, const int *__restrict__ alive,
-                          const int *__restrict__ start, int *__restrict__ fill, int *__restrict__ list)
+                          const int *__restrict__ start, int *__restrict__ fill, int *__restrict__ list,
+                          const int *__restrict__ active)
 {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   if (alive && !alive[i]) return;
+  if (active && !active[i]) return;
   int c = cell[i];
   if (c < 0) return;
   int pos = start[c] + atomicAdd(&fill[c], 1);
@@ -166,7 +169,7 @@ extern "C" int lgb_op_scatter(int n, const int *cell, const int *alive, const in
                               void *stream)
 {
   if (n <= 0) return 0;
-  k_scatter<<<lgb_cdiv(n, 256), 256, 0, (cudaStream_t)stream>>>(n, cell, alive, start, fill, list);
+  k_scatter<<<lgb_cdiv(n, 256), 256, 0, (cudaStream_t)stream>>>(n, cell, alive, start, fill, list, NULL);
   lgb_count_launch(1);
   LGB_CHECK_LAUNCH();
   return 0;
@@ -338,15 +341,28 @@ __global__ void k_chunks(int ncells, int cap, const int *__restrict__ pstart, in
 
 extern "C" int lgb_op_bin_particles(lgb_dev *d, int mark_dead, void *stream)
 {
+  return lgb_op_bin_particles_mask(d, mark_dead, NULL, stream);
+}
+
+extern "C" int lgb_op_bin_particles_mask(lgb_dev *d, int mark_dead, const int *active, void *stream)
+{
   cudaStream_t s = (cudaStream_t)stream;
   const lgb_geom &g = d->g;
   int rc;
   cudaMemsetAsync(d->pcount, 0, sizeof(int) * (g.ncells + 1), s);
   cudaMemsetAsync(d->pfill, 0, sizeof(int) * g.ncells, s);
-  if ((rc = lgb_op_locate(&g, d->np, d->xp, d->cell_p, mark_dead ? d->alive : NULL, d->pcount, NULL, stream)))
-    return rc;
+  if (d->np > 0) {
+    k_locate<<<lgb_cdiv(d->np, 256), 256, 0, s>>>(g, d->np, d->xp, d->cell_p, mark_dead ? d->alive : NULL, d->pcount,
+                                                   NULL, active);
+    lgb_count_launch(1);
+    LGB_CHECK_LAUNCH();
+  }
   if ((rc = lgb_op_scan_i32(g.ncells, d->pcount, d->pstart, d->scan_tmp, stream))) return rc;
-  if ((rc = lgb_op_scatter(d->np, d->cell_p, d->alive, d->pstart, d->pfill, d->plist, stream))) return rc;
+  if (d->np > 0) {
+    k_scatter<<<lgb_cdiv(d->np, 256), 256, 0, s>>>(d->np, d->cell_p, d->alive, d->pstart, d->pfill, d->plist, active);
+    lgb_count_launch(1);
+    LGB_CHECK_LAUNCH();
+  }
   k_chunks<<<lgb_cdiv(g.ncells, 256), 256, 0, s>>>(g.ncells, d->chunk_cap, d->pstart, d->pfill);
   lgb_count_launch(1);
   LGB_CHECK_LAUNCH();

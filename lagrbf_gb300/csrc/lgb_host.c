@@ -293,6 +293,7 @@ static void free_particles(lgb_dev *d)
 {
   DFREE(d->xp); DFREE(d->fields); DFREE(d->vel); DFREE(d->x0); DFREE(d->vadv);
   DFREE(d->cell_p); DFREE(d->alive); DFREE(d->plist);
+  DFREE(d->tp); DFREE(d->hp); DFREE(d->hcur); DFREE(d->active);
   d->np_cap = 0;
 }
 
@@ -464,6 +465,8 @@ static int read_options(lgb_ctx *c)
   opt_real("dopri_dt_fac_max", &c->dopri[2]);
   opt_real("dopri_atol", &c->dopri[3]);
   opt_real("dopri_rtol", &c->dopri[4]);
+  d->dopri_pp = 0;
+  opt_bool("dopri_per_particle", &d->dopri_pp);
   d->prec = LGB_PREC_FP64;
   if (opt_str("eval_precision", buf, sizeof(buf))) {
     if (strcmp(buf, "fp32") == 0) d->prec = LGB_PREC_FP32;
@@ -861,6 +864,12 @@ static int fill_points(lgb_ctx *c, int n, const double *coords, const double *va
     d->cell_p = (int *)dalloc(sizeof(int) * (size_t)n, &err);
     d->alive = (int *)dalloc(sizeof(int) * (size_t)n, &err);
     d->plist = (int *)dalloc(sizeof(int) * (size_t)n, &err);
+    if (d->dopri_pp) {
+      d->tp = (double *)dalloc(sizeof(double) * (size_t)n, &err);
+      d->hp = (double *)dalloc(sizeof(double) * (size_t)n, &err);
+      d->hcur = (double *)dalloc(sizeof(double) * 2 * (size_t)n, &err);
+      d->active = (int *)dalloc(sizeof(int) * (size_t)n, &err);
+    }
     if (err) { DFREE(of); DFREE(ov); return set_error(LAGRBF_ERR_MEM, "particle swarm allocation failed (%d points)", n); }
     CU(cudaMemsetAsync(d->fields, 0, sizeof(double) * (size_t)n * (F ? F : 1), c->stream));
     CU(cudaMemsetAsync(d->vel, 0, sizeof(double) * (size_t)n * dim, c->stream));
@@ -876,6 +885,8 @@ static int fill_points(lgb_ctx *c, int n, const double *coords, const double *va
   }
   if (n != old) invalidate_graph(c);
   d->np = n;
+  /* a new particle set starts per-particle Dormand-Prince from the context step */
+  if (d->dopri_pp && n > 0) CU(cudaMemsetAsync(d->hp, 0, sizeof(double) * (size_t)n, c->stream));
   if (n > 0) {
     int i, *ones = (int *)malloc(sizeof(int) * (size_t)n);
     cudaError_t e = cudaSuccess;
@@ -1020,7 +1031,8 @@ static int step_sequence(lgb_ctx *c, int analytical)
   lgb_dev *d = &c->d;
   void *s = c->stream;
   int st;
-  OP(lgb_op_ctrl(d, LGB_CTRL_BEGIN_STEP, s));
+  const int pp = (c->scheme == LGB_DOPRI && d->dopri_pp);
+  OP(lgb_op_ctrl(d, pp ? LGB_CTRL_BEGIN_SWEEP : LGB_CTRL_BEGIN_STEP, s));
   switch (c->scheme) {
   case LGB_RK1:
     OP(lgb_op_stage(d, LGB_RK1, 0, s));
@@ -1043,6 +1055,18 @@ static int step_sequence(lgb_ctx *c, int analytical)
     OP(lgb_op_bin_particles(d, 1, s));
     break;
   case LGB_DOPRI:
+    if (pp) {
+      /* per-particle steps: only the particles still short of t_next are staged and evaluated */
+      OP(lgb_op_pp_begin(d, s));
+      for (st = 0; st < 6; st++) {
+        OP(lgb_op_stage(d, LGB_DOPRI, st, s));
+        OP(lgb_op_bin_particles_mask(d, 1, d->active, s));
+        TRY(eval_velocity(c, analytical));
+      }
+      OP(lgb_op_pp_accept(d, s));
+      OP(lgb_op_bin_particles(d, 1, s)); /* rejected particles are back at x0 */
+      break;
+    }
     for (st = 0; st < 6; st++) {
       OP(lgb_op_stage(d, LGB_DOPRI, st, s));
       OP(lgb_op_bin_particles(d, 1, s));
@@ -1064,7 +1088,7 @@ static int step_sequence(lgb_ctx *c, int analytical)
     OP(lgb_op_ctrl(d, LGB_CTRL_RESET_CFL, s));
     OP(lgb_op_count_alive(d, s));
   }
-  OP(lgb_op_ctrl(d, LGB_CTRL_END_STEP, s));
+  OP(lgb_op_ctrl(d, pp ? LGB_CTRL_END_SWEEP : LGB_CTRL_END_STEP, s));
   return 0;
 }
 
@@ -1137,6 +1161,7 @@ static int advection_loop(lgb_ctx *c, double t, double t_next, int analytical, i
   c->hctrl->t = t;
   c->hctrl->t_next = t_next;
   c->hctrl->scheme = c->scheme;
+  c->hctrl->pp_hmin = 1e-10 * (t_next - t);
   CU(cudaMemcpyAsync(d->ctrl, c->hctrl, sizeof(lgb_ctrl), cudaMemcpyHostToDevice, c->stream));
   /* AdvectionInitializeTimestepVelocity, then the CFL of that velocity */
   OP(lgb_op_ctrl(d, LGB_CTRL_RESET_CFL, c->stream));
@@ -1146,6 +1171,7 @@ static int advection_loop(lgb_ctx *c, double t, double t_next, int analytical, i
   } else {
     OP(lgb_op_copy_velocity(d, c->stream));
   }
+  if (c->scheme == LGB_DOPRI && d->dopri_pp) OP(lgb_op_pp_init(d, t, c->stream));
   CU(cudaStreamSynchronize(c->stream));
   while (t < t_next) {
     TRY(run_step(c, analytical));

@@ -102,6 +102,8 @@ typedef struct {
   int nfactored;
   double factor_flops;
   int eval_error;      /* a bounded wait of the evaluation kernel gave up */
+  int pp_left;         /* per-particle Dormand-Prince: particles still short of t_next   */
+  double pp_hmin;      /* per-particle Dormand-Prince: steps below this are accepted      */
 } lgb_ctrl;
 
 typedef struct {
@@ -127,6 +129,11 @@ typedef struct {
   double *ws;          /* factorisation workspace: nws slots of ws_stride doubles */
   double *kappa;       /* per-patch 1-norm condition estimates (nnodes), when cond_on    */
   int cond_on;
+  /* per-particle adaptive Dormand-Prince (option dopri_per_particle): time reached, next step, step
+     of the current sweep, and whether the particle takes part in the sweep */
+  int dopri_pp;
+  double *tp, *hp, *hcur;
+  int *active;
   long long ws_stride;
   int nws;
   /* particle swarm */
@@ -165,6 +172,8 @@ int lgb_op_scatter(int n, const int *cell, const int *alive, const int *start, i
 int lgb_op_data_arrange(lgb_dev *d, void *stream);      /* xs, xr, fs, patch sizes, slots, offsets */
 int lgb_op_data_values(lgb_dev *d, void *stream);       /* fs only (values changed)                */
 int lgb_op_bin_particles(lgb_dev *d, int mark_dead, void *stream); /* cell_p, pcount, pstart, plist, chunks */
+/* the same, listing for evaluation only the particles with active[p] != 0 (all are located) */
+int lgb_op_bin_particles_mask(lgb_dev *d, int mark_dead, const int *active, void *stream);
 int lgb_op_mark_patches(lgb_dev *d, void *stream);      /* queue patches touched by live particles */
 /* lgb_factor.cu */
 int lgb_op_factor(lgb_dev *d, void *stream);            /* set up / solve queued patches */
@@ -176,7 +185,13 @@ int lgb_op_build_records(lgb_dev *d, int force, void *stream);
 int lgb_op_stage(lgb_dev *d, int scheme, int stage, void *stream);
 int lgb_op_dopri_error(lgb_dev *d, void *stream);
 int lgb_op_ctrl(lgb_dev *d, int what, void *stream);
-enum { LGB_CTRL_BEGIN_STEP = 0, LGB_CTRL_END_STEP = 1, LGB_CTRL_RESET_CFL = 2, LGB_CTRL_DOPRI_DT = 3 };
+enum { LGB_CTRL_BEGIN_STEP = 0, LGB_CTRL_END_STEP = 1, LGB_CTRL_RESET_CFL = 2, LGB_CTRL_DOPRI_DT = 3,
+       LGB_CTRL_BEGIN_SWEEP = 4, LGB_CTRL_END_SWEEP = 5 };
+/* per-particle Dormand-Prince: tp = t (and hp = dt_adv where unset); the sweep's steps; the error,
+   acceptance and next step of every particle in the sweep */
+int lgb_op_pp_init(lgb_dev *d, double t, void *stream);
+int lgb_op_pp_begin(lgb_dev *d, void *stream);
+int lgb_op_pp_accept(lgb_dev *d, void *stream);
 int lgb_op_copy_velocity(lgb_dev *d, void *stream);     /* vel <- fields[:, :dim] */
 int lgb_op_count_alive(lgb_dev *d, void *stream);
 int lgb_op_velocity_field(lgb_dev *d, void *stream);    /* vel <- analytical field at live particles */

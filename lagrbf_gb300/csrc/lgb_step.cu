@@ -44,14 +44,17 @@ struct StageParams {
   double *xp, *x0, *vel, *vadv;
   const int *alive;
   const lgb_ctrl *ctrl;
+  const double *hcur;  /* per-particle Dormand-Prince: the particle's step (else NULL: ctrl->dt) */
+  const int *active;   /* per-particle Dormand-Prince: particles taking part in the sweep      */
 };
 
 __global__ void k_stage(StageParams S)
 {
   int p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= S.np || !S.alive[p]) return;
+  if (S.active && !S.active[p]) return;
   const int dim = S.dim;
-  const double dt = S.ctrl->dt;
+  const double dt = S.hcur ? S.hcur[p] : S.ctrl->dt;
   const double rmin = S.ctrl->rmin, rmax = S.ctrl->rmax;
   const size_t o = (size_t)p * dim;
   const size_t st = (size_t)S.np * dim; /* stride between v_adv stages */
@@ -121,6 +124,9 @@ extern "C" int lgb_op_stage(lgb_dev *d, int scheme, int stage, void *stream)
   StageParams S;
   S.np = d->np; S.dim = d->g.dim; S.scheme = scheme; S.stage = stage;
   S.xp = d->xp; S.x0 = d->x0; S.vel = d->vel; S.vadv = d->vadv; S.alive = d->alive; S.ctrl = d->ctrl;
+  const int pp = (scheme == LGB_DOPRI && d->dopri_pp);
+  S.hcur = pp ? d->hcur : NULL;
+  S.active = pp ? d->active : NULL;
   k_stage<<<lgb_cdiv(d->np, 256), 256, 0, (cudaStream_t)stream>>>(S);
   lgb_count_launch(1);
   return (int)cudaGetLastError();
@@ -172,6 +178,143 @@ extern "C" int lgb_op_dopri_error(lgb_dev *d, void *stream)
   if (d->np <= 0) return 0;
   k_dopri_error<<<lgb_cdiv(d->np, 256), 256, 0, (cudaStream_t)stream>>>(d->np, d->g.dim, d->xp, d->x0, d->vel,
                                                                           d->vadv, d->alive, d->ctrl);
+  lgb_count_launch(1);
+  return (int)cudaGetLastError();
+}
+
+/* ---- per-particle adaptive Dormand-Prince (an extension: the reference's scheme takes one global
+   step from the global maximum error and always accepts it, dormand_prince.c:93,179-214).  Every
+   live particle short of t_next attempts h_p = min(hp_p, its own CFL step cfl r / (|v_p| + 1e-16),
+   t_next - tp_p) through the same six stages; the stage evaluations see only those particles.  The
+   error norm E_p is the reference's (dormand_prince.c:68-91) for that particle; E_p <= 1 (or
+   h_p < hmin, so that no particle stalls) accepts the step, else the particle returns to x0; either
+   way hp_p = h_p min(fac_max', max(fac_min, fac E_p^-1/5)), fac_max' = fac_max after an accepted
+   step and 1 after a rejected one. ---- */
+__global__ void k_pp_init(int np, const int *__restrict__ alive, double *__restrict__ tp, double *__restrict__ hp,
+                          double t, const lgb_ctrl *ctrl)
+{
+  int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= np) return;
+  tp[p] = t;
+  if (!(hp[p] > 0.0)) hp[p] = ctrl->dt_adv;
+}
+
+__global__ void k_pp_begin(int np, int dim, const int *__restrict__ alive, const double *__restrict__ vel,
+                           const double *__restrict__ tp, const double *__restrict__ hp, double *__restrict__ hcur,
+                           int *__restrict__ active, const lgb_ctrl *ctrl)
+{
+  int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= np) return;
+  const double t_next = ctrl->t_next;
+  const int act = alive[p] && tp[p] < t_next;
+  active[p] = act;
+  double h = 0.0;
+  if (act) {
+    double n2 = 0.0;
+    for (int d = 0; d < dim; d++) n2 += vel[(size_t)p * dim + d] * vel[(size_t)p * dim + d];
+    const double cfl = ctrl->cfl_fac * ctrl->cfl_radius / (sqrt(n2) + 1e-16);
+    h = (hp[p] < cfl) ? hp[p] : cfl;
+    if (tp[p] + h >= t_next) h = -(t_next - tp[p]); /* negative: clamped to t_next */
+  }
+  hcur[p] = h;
+}
+
+/* The stages read |hcur|; the sign marks a step clamped to t_next. */
+__global__ void k_pp_abs(int np, double *__restrict__ hcur, double *__restrict__ hsign)
+{
+  int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= np) return;
+  const double h = hcur[p];
+  hsign[p] = h;
+  hcur[p] = fabs(h);
+}
+
+__global__ void k_pp_accept(int np, int dim, double *__restrict__ xp, const double *__restrict__ x0,
+                            const double *__restrict__ vel, double *__restrict__ vadv, const int *__restrict__ alive,
+                            const int *__restrict__ active, double *__restrict__ tp, double *__restrict__ hp,
+                            const double *__restrict__ hsign, lgb_ctrl *ctrl)
+{
+  int p = blockIdx.x * blockDim.x + threadIdx.x;
+  int acc = 0, left = 0;
+  if (p < np && alive[p] && active[p]) {
+    const size_t o = (size_t)p * dim, st = (size_t)np * dim;
+    const double hs = hsign[p], h = fabs(hs), atol = ctrl->dopri_atol, rtol = ctrl->dopri_rtol;
+    for (int d = 0; d < dim; d++) vadv[6 * st + o + d] = vel[o + d];
+    double vlow[3] = {0.0, 0.0, 0.0};
+    for (int i = 0; i < 7; i++)
+      for (int d = 0; d < dim; d++) vlow[d] += c_dp_e[i] * vadv[i * st + o + d];
+    double e2 = 0.0;
+    for (int d = 0; d < dim; d++) {
+      const double xa = x0[o + d], xb = xp[o + d];
+      const double mv = (fabs(xa) < fabs(xb)) ? fabs(xb) : fabs(xa);
+      const double tol = atol + rtol * mv;
+      const double err = xb - (xa + h * vlow[d]);
+      e2 += (err * err) / (tol * tol);
+    }
+    const double E = sqrt(1.0 / dim * e2);
+    acc = (E <= 1.0) || (h < ctrl->pp_hmin);
+    if (acc) {
+      tp[p] = (hs < 0.0) ? ctrl->t_next : tp[p] + h;
+    } else {
+      for (int d = 0; d < dim; d++) xp[o + d] = x0[o + d];
+    }
+    const double fmx = (E <= 1.0) ? ctrl->dopri_fac_max : 1.0;
+    const double q = ctrl->dopri_fac * pow(1.0 / E, 1.0 / 5.0);
+    const double inner = (ctrl->dopri_fac_min < q) ? q : ctrl->dopri_fac_min;
+    hp[p] = h * ((fmx < inner) ? fmx : inner);
+    left = tp[p] < ctrl->t_next;
+  } else if (p < np && alive[p]) {
+    left = tp[p] < ctrl->t_next;
+  }
+  /* block sums, then one atomic each per block */
+  __shared__ int s_a[32], s_l[32];
+  for (int off = 16; off > 0; off >>= 1) {
+    acc += __shfl_down_sync(0xffffffffu, acc, off);
+    left += __shfl_down_sync(0xffffffffu, left, off);
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+  if (lane == 0) { s_a[warp] = acc; s_l[warp] = left; }
+  __syncthreads();
+  if (warp == 0) {
+    acc = (lane < nw) ? s_a[lane] : 0;
+    left = (lane < nw) ? s_l[lane] : 0;
+    for (int off = 16; off > 0; off >>= 1) {
+      acc += __shfl_down_sync(0xffffffffu, acc, off);
+      left += __shfl_down_sync(0xffffffffu, left, off);
+    }
+    if (lane == 0) {
+      if (acc) atomicAdd((unsigned long long *)&ctrl->particle_steps, (unsigned long long)acc);
+      if (left) atomicAdd(&ctrl->pp_left, left);
+    }
+  }
+}
+
+extern "C" int lgb_op_pp_init(lgb_dev *d, double t, void *stream)
+{
+  if (d->np <= 0) return 0;
+  k_pp_init<<<lgb_cdiv(d->np, 256), 256, 0, (cudaStream_t)stream>>>(d->np, d->alive, d->tp, d->hp, t, d->ctrl);
+  lgb_count_launch(1);
+  return (int)cudaGetLastError();
+}
+
+extern "C" int lgb_op_pp_begin(lgb_dev *d, void *stream)
+{
+  if (d->np <= 0) return 0;
+  cudaStream_t s = (cudaStream_t)stream;
+  /* hcur has 2 np entries: the stages read |h| from the first half, the acceptance the signed step
+     (negative: clamped to t_next) from the second */
+  k_pp_begin<<<lgb_cdiv(d->np, 256), 256, 0, s>>>(d->np, d->g.dim, d->alive, d->vel, d->tp, d->hp, d->hcur, d->active,
+                                                 d->ctrl);
+  k_pp_abs<<<lgb_cdiv(d->np, 256), 256, 0, s>>>(d->np, d->hcur, d->hcur + d->np);
+  lgb_count_launch(2);
+  return (int)cudaGetLastError();
+}
+
+extern "C" int lgb_op_pp_accept(lgb_dev *d, void *stream)
+{
+  if (d->np <= 0) return 0;
+  k_pp_accept<<<lgb_cdiv(d->np, 256), 256, 0, (cudaStream_t)stream>>>(
+      d->np, d->g.dim, d->xp, d->x0, d->vel, d->vadv, d->alive, d->active, d->tp, d->hp, d->hcur + d->np, d->ctrl);
   lgb_count_launch(1);
   return (int)cudaGetLastError();
 }
@@ -340,6 +483,13 @@ __global__ void k_ctrl(lgb_ctrl *c, int what)
     c->t += c->dt;
     c->steps += 1;
     c->particle_steps += c->np_alive;
+    break;
+  case LGB_CTRL_BEGIN_SWEEP:
+    c->pp_left = 0;
+    break;
+  case LGB_CTRL_END_SWEEP: /* accepted particle steps are counted by k_pp_accept */
+    if (c->pp_left == 0) c->t = c->t_next;
+    c->steps += 1;
     break;
   default: break;
   }

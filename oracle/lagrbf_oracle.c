@@ -617,6 +617,10 @@ struct orc_ctx {
   double dt;             /* AdvectionCtx dt; DOPRI writes its adapted step here */
   double dopri_error;
   int nsteps;
+  /* per-particle Dormand-Prince (extension): time reached, next step, step of the sweep */
+  double *tp, *hp, *hcur;
+  int *act, *clamped;
+  long long pp_accepted;
   orc_velocity_fn vfn;
   orc_velocity_batch_fn vfn_batch;
   void *vuser;
@@ -670,6 +674,7 @@ void orc_destroy(orc_ctx *c)
   free(c->xp); free(c->fields); free(c->vel); free(c->weights); free(c->x0);
   for (s = 0; s < 7; s++) free(c->vadv[s]);
   free(c->pid_p); free(c->cell_p); free(c->alive);
+  free(c->tp); free(c->hp); free(c->hcur); free(c->act); free(c->clamped);
   free(c);
 }
 
@@ -744,6 +749,12 @@ int orc_fill_swarm(orc_ctx *c, int is_data, int n, const double *coords, const d
     c->pid_p = (int64_t *)xrealloc(c->pid_p, sizeof(int64_t) * (size_t)(n ? n : 1));
     c->cell_p = (int *)xrealloc(c->cell_p, sizeof(int) * (size_t)(n ? n : 1));
     c->alive = (int *)xrealloc(c->alive, sizeof(int) * (size_t)(n ? n : 1));
+    c->tp = (double *)xrealloc(c->tp, sizeof(double) * (size_t)(n ? n : 1));
+    c->hp = (double *)xrealloc(c->hp, sizeof(double) * (size_t)(n ? n : 1));
+    c->hcur = (double *)xrealloc(c->hcur, sizeof(double) * (size_t)(n ? n : 1));
+    c->act = (int *)xrealloc(c->act, sizeof(int) * (size_t)(n ? n : 1));
+    c->clamped = (int *)xrealloc(c->clamped, sizeof(int) * (size_t)(n ? n : 1));
+    for (p = 0; p < n; p++) c->hp[p] = 0.0; /* a new swarm starts from the context step */
     for (p = old; p < n; p++) c->pid_p[p] = 0;
     if (n > old) {
       memset(&c->fields[(size_t)old * F], 0, sizeof(double) * (size_t)(n - old) * F);
@@ -1081,6 +1092,78 @@ static int dopri(orc_ctx *c)
   return 0;
 }
 
+/* Per-particle adaptive Dormand-Prince, one sweep (an extension; the reference's scheme above takes
+   one global step from the global maximum error and always accepts it).  Every live particle p
+   short of t_next attempts a step h_p = min(hp_p, its own CFL step cfl r / (|v_p| + 1e-16),
+   t_next - tp_p) with the same stages and error norm E_p as dormand_prince.c:37-102, 216-310; the
+   step is accepted when E_p <= 1 (or when h_p has fallen below hmin, so that no particle stalls),
+   else the particle returns to x0; either way hp_p = h_p min(fac_max', max(fac_min, fac E_p^-1/5))
+   with fac_max' = fac_max after an accepted step and 1 after a rejected one (dormand_prince.c:
+   179-214 per particle).  Particles that are done keep their position; their stage velocities are
+   evaluated but unused. */
+static int dopri_pp_sweep(orc_ctx *c, double t_next, double hmin)
+{
+  int dim = c->pu.dim, s, j, p, d, err;
+  const double radius = 1.0 / c->pu.eps_w;
+  for (p = 0; p < c->np; p++) {
+    double nv = 0.0, h, cfl;
+    c->act[p] = c->alive[p] && c->tp[p] < t_next;
+    c->clamped[p] = 0;
+    c->hcur[p] = 0.0;
+    if (!c->act[p]) continue;
+    for (d = 0; d < dim; d++) nv += c->vel[(size_t)p * dim + d] * c->vel[(size_t)p * dim + d];
+    cfl = c->cfg.cfl_fac * radius / (sqrt(nv) + 1e-16);
+    h = ORC_MIN(c->hp[p], cfl);
+    if (c->tp[p] + h >= t_next) { h = t_next - c->tp[p]; c->clamped[p] = 1; }
+    c->hcur[p] = h;
+  }
+  set_initial_values(c);
+  for (s = 0; s < 6; s++) {
+    int stage = s + 1;
+    for (p = 0; p < c->np; p++) {
+      if (!c->alive[p] || !c->act[p]) continue;
+      for (d = 0; d < dim; d++) c->vel[(size_t)p * dim + d] = 0.0;
+      for (j = 0; j < stage; j++)
+        for (d = 0; d < dim; d++) c->vel[(size_t)p * dim + d] += DP_A[s][j] * c->vadv[j][(size_t)p * dim + d];
+      for (d = 0; d < dim; d++)
+        c->xp[(size_t)p * dim + d] = c->x0[(size_t)p * dim + d] + c->hcur[p] * c->vel[(size_t)p * dim + d];
+      project_sphere(&c->xp[(size_t)p * dim], dim, c->cfg.rmin, c->cfg.rmax);
+    }
+    migrate_and_weights(c);
+    if ((err = evaluate_velocity(c))) return err;
+    memcpy(c->vadv[stage], c->vel, sizeof(double) * (size_t)c->np * dim);
+  }
+  for (p = 0; p < c->np; p++) {
+    double vlow[3] = {0.0, 0.0, 0.0}, E = 0.0, h = c->hcur[p], fmax, f;
+    int acc;
+    if (!c->act[p] || !c->alive[p]) continue;
+    for (s = 0; s < 7; s++)
+      for (d = 0; d < dim; d++) vlow[d] += DP_E[s] * c->vadv[s][(size_t)p * dim + d];
+    for (d = 0; d < dim; d++) {
+      double x0 = c->x0[(size_t)p * dim + d], x = c->xp[(size_t)p * dim + d];
+      double mv = ORC_MAX(fabs(x0), fabs(x));
+      double tol = c->cfg.dopri_atol + c->cfg.dopri_rtol * mv;
+      double e = x - (x0 + h * vlow[d]);
+      E += (e * e) / (tol * tol);
+    }
+    E = sqrt(1.0 / dim * E);
+    acc = (E <= 1.0) || (h < hmin);
+    if (acc) {
+      c->tp[p] = c->clamped[p] ? t_next : c->tp[p] + h;
+      c->pp_accepted++;
+    } else {
+      for (d = 0; d < dim; d++) c->xp[(size_t)p * dim + d] = c->x0[(size_t)p * dim + d];
+    }
+    fmax = (E <= 1.0) ? c->cfg.dopri_dt_fac_max : 1.0;
+    f = ORC_MIN(fmax, ORC_MAX(c->cfg.dopri_dt_fac_min, c->cfg.dopri_dt_fac * pow(1.0 / E, 1.0 / 5.0)));
+    c->hp[p] = h * f;
+  }
+  migrate_and_weights(c);
+  return 0;
+}
+
+long long orc_get_accepted(orc_ctx *c) { return c->pp_accepted; }
+
 static int advect_swarm(orc_ctx *c)
 {
   switch (c->cfg.scheme) {
@@ -1113,7 +1196,26 @@ static int advection_loop(orc_ctx *c, double t, double t_next, int interpolated,
   /* InternalForwardAdvectionLoop (time_loop.c:39-100) / ForwardAnalyticalAdvection (:176-221) */
   int err;
   if ((err = initialize_timestep_velocity(c))) return err;
-  while (t < t_next) {
+  if (c->cfg.scheme == ORC_DOPRI && c->cfg.dopri_per_particle) {
+    const double hmin = 1e-10 * (t_next - t);
+    int p, left = 1;
+    for (p = 0; p < c->np; p++) {
+      c->tp[p] = t;
+      if (!(c->hp[p] > 0.0)) c->hp[p] = c->dt;
+    }
+    while (left) {
+      if ((err = dopri_pp_sweep(c, t_next, hmin))) return err;
+      if (interpolated) {
+        if ((err = partitions_setup(c))) return err;
+        rbf_interpolation(c, c->cfg.nfields, c->fields);
+      }
+      if ((err = initialize_timestep_velocity(c))) return err;
+      c->nsteps++;
+      left = 0;
+      for (p = 0; p < c->np; p++) left |= c->alive[p] && c->tp[p] < t_next;
+    }
+  }
+  while (t < t_next && !(c->cfg.scheme == ORC_DOPRI && c->cfg.dopri_per_particle)) {
     double dt;
     if (c->cfg.scheme == ORC_DOPRI) {
       double dt_cfl = cfl_dt(c);

@@ -42,6 +42,8 @@ typedef struct {
   int    scheme;       /* advection_scheme                                        */
   double cfl_fac, dt, rmin, rmax;
   double dopri_dt_fac, dopri_dt_fac_min, dopri_dt_fac_max, dopri_atol, dopri_rtol;
+  int    dopri_per_particle; /* extension: per-particle adaptive Dormand-Prince (0: the reference's
+                                single global step, always accepted)                              */
 } orc_config;
 
 /* Defaults of LagRBFCtxCreate (src/lagrangian_rbf.c:36-73), AdvectionCtxCreate
@@ -99,6 +101,8 @@ void orc_eval(const orc_pu *pu, int kernel, int np, const double *xp, const int 
 
 /* ---------------- reference-API emulation ---------------- */
 typedef struct orc_ctx orc_ctx;
+/* Accepted particle steps of per-particle Dormand-Prince since the context was created. */
+long long orc_get_accepted(orc_ctx *c);
 typedef int (*orc_velocity_fn)(double *coords, double *velocity, void *user);
 typedef int (*orc_velocity_batch_fn)(int32_t npoints, int32_t dim, double *coords, double *velocity, void *user);
 

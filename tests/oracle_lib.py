@@ -22,7 +22,7 @@ class OrcConfig(ctypes.Structure):
         ("scheme", ctypes.c_int), ("cfl_fac", ctypes.c_double), ("dt", ctypes.c_double),
         ("rmin", ctypes.c_double), ("rmax", ctypes.c_double), ("dopri_dt_fac", ctypes.c_double),
         ("dopri_dt_fac_min", ctypes.c_double), ("dopri_dt_fac_max", ctypes.c_double),
-        ("dopri_atol", ctypes.c_double), ("dopri_rtol", ctypes.c_double),
+        ("dopri_atol", ctypes.c_double), ("dopri_rtol", ctypes.c_double), ("dopri_per_particle", ctypes.c_int),
     ]
 
 
@@ -81,6 +81,8 @@ def lib():
         L.orc_advect_analytical.argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.c_double]
         L.orc_set_velocity_batch_fn.argtypes = [ctypes.c_void_p, VFN_BATCH, ctypes.c_void_p]
         L.orc_get_counts.argtypes = [ctypes.c_void_p] + [ctypes.POINTER(ctypes.c_int)] * 4
+        L.orc_get_accepted.restype = ctypes.c_longlong
+        L.orc_get_accepted.argtypes = [ctypes.c_void_p]
         L.orc_get_dt.restype = ctypes.c_double
         L.orc_get_dt.argtypes = [ctypes.c_void_p]
         L.orc_get_cellids.argtypes = [ctypes.c_void_p, ctypes.c_int, i]
@@ -115,7 +117,7 @@ def lib():
 
 def make_config(dim, npartitions, nfields, kernel=2, overlap=1.0, shape_factor=1.0, minCoords=None,
                 maxCoords=None, solve_method=2, advection=False, advection_scheme=2, advection_cfl=0.3,
-                dt=1e-4, rmin=0.0, rmax=1e132, **_):
+                dt=1e-4, rmin=0.0, rmax=1e132, dopri_per_particle=False, dopri_rtol=None, dopri_atol=None, **_):
     """Config with the lagrbfpy keyword defaults (context.py:113-201)."""
     c = OrcConfig()
     lib().orc_config_default(ctypes.byref(c))
@@ -126,6 +128,11 @@ def make_config(dim, npartitions, nfields, kernel=2, overlap=1.0, shape_factor=1
         c.L[k] = 1.0 if maxCoords is None else maxCoords[k]
     c.overlap, c.shape_factor, c.kernel, c.solve_method, c.nfields = overlap, shape_factor, kernel, solve_method, nfields
     c.advection, c.scheme, c.cfl_fac, c.dt, c.rmin, c.rmax = int(advection), advection_scheme, advection_cfl, dt, rmin, rmax
+    c.dopri_per_particle = int(bool(dopri_per_particle))
+    if dopri_rtol is not None:
+        c.dopri_rtol = dopri_rtol
+    if dopri_atol is not None:
+        c.dopri_atol = dopri_atol
     return c
 
 
@@ -186,6 +193,9 @@ class Oracle:
 
     def dt(self):
         return lib().orc_get_dt(self.h)
+
+    def accepted(self):
+        return lib().orc_get_accepted(self.h)
 
     def cellids(self, is_data, n):
         out = np.zeros(n, dtype=np.int32)

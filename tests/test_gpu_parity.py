@@ -544,3 +544,48 @@ def test_empty_swarms():
     x2, f2, p2 = o.output(len(xp))
     assert np.array_equal(p1, p2) and np.array_equal(x1, x2) and np.array_equal(f1, f2)
     assert not f1.any()
+
+
+@pytest.mark.parametrize("field", ["interpolated", "rotation"])
+def test_per_particle_dopri_matches_oracle(field):
+    """Per-particle adaptive Dormand-Prince (extension, option dopri_per_particle): every particle
+    takes its own CFL-limited step with the reference's error norm, accept/reject and step update;
+    the GPU and the oracle take the same sweeps and accept the same particle steps, and end at the
+    same positions."""
+    xd, fd, xp, opts = small_3d(np_=1500)
+    adv = dict(advection=True, advection_scheme=3, advection_cfl=0.3, dt=2e-3, solve_method=1)
+    popt = {"dopri_per_particle": True, "dopri_rtol": 1e-7, "dopri_atol": 1e-9}
+    c = gpu_ctx(opts, **adv, petsc_options=popt)
+    o = Oracle(**opts, **adv, dopri_per_particle=True, dopri_rtol=1e-7, dopri_atol=1e-9)
+    t, dt = 0.0, 6e-3
+    c.fill_points(xp)
+    assert o.fill(False, xp) == 0
+    if field == "rotation":
+        rot = lambda n, d, x, v, u: _rot3(n, d, x, v)  # noqa: E731
+        c.set_velocity_field(c.VFIELD_ROTATION, [2.0, 0.5, 0.5])
+        assert o.set_velocity_batch(rot) == 0
+    for _ in range(2):
+        if field == "interpolated":
+            c.fill_data(xd, fd); c.interpolate_c()
+            assert o.fill(True, xd, fd) == 0 and o.interpolate() == 0
+            c.advect_interpolate_c(t, t + dt)
+            assert o.advect(t, t + dt) == 0
+        else:
+            c.advect_analytical_c(t, t + dt)
+            assert o.advect_analytical(t, t + dt) == 0
+        t += dt
+    x1, _, p1 = gpu_output(c, len(xp), 3)
+    x2, _, p2 = o.output(len(xp))
+    assert np.array_equal(p1, p2)
+    st = c.stats()
+    assert st["steps"] == o.counts()[3]
+    assert st["particle_steps"] == o.accepted()
+    assert np.abs(x1 - x2).max() <= 1e-11
+
+
+def _rot3(n, dim, x, v):
+    for p in range(n):
+        v[dim * p] = -2.0 * (x[dim * p + 1] - 0.5)
+        v[dim * p + 1] = 2.0 * (x[dim * p] - 0.5)
+        v[dim * p + 2] = 0.0
+    return 0

@@ -153,3 +153,31 @@ def test_analytical_advection_without_fields():
     assert o.advect_analytical(0.0, 0.3) == 0
     x, _, _ = o.output(len(xp), fieldname="velocity")
     assert np.all(np.isfinite(x)) and np.abs(x - xp).max() > 0.0
+
+
+def _rotation_radii(per_particle, cfl=0.1, t_end=1.2):
+    """Rigid rotation of particles at radii 0.02-0.4 (speeds 0.02-0.4): returns the max position
+    error, internal steps (sweeps) and accepted particle steps."""
+    r = np.linspace(0.02, 0.4, 24)
+    a = np.linspace(0, 2 * np.pi, 24, endpoint=False)
+    xp = 0.5 + np.stack([r * np.cos(a), r * np.sin(a)], 1)
+    o = Oracle(dim=2, npartitions=[5, 5], nfields=2, overlap=W.pu_overlap(5), kernel=2, advection=True,
+               advection_scheme=3, advection_cfl=cfl, dopri_per_particle=per_particle, dopri_rtol=1e-8,
+               dopri_atol=1e-10)
+    assert o.set_velocity_batch(_rotation_batch) == 0
+    assert o.fill(False, xp) == 0
+    assert o.advect_analytical(0.0, t_end) == 0
+    x, _, _ = o.output(len(xp), fieldname="velocity")
+    c, s = np.cos(t_end), np.sin(t_end)
+    exact = 0.5 + np.stack([c * (xp[:, 0] - 0.5) - s * (xp[:, 1] - 0.5), s * (xp[:, 0] - 0.5) + c * (xp[:, 1] - 0.5)], 1)
+    return np.abs(x - exact).max(), o.counts()[3], o.accepted()
+
+
+def test_dopri_per_particle_meets_tolerance_with_fewer_particle_steps():
+    """Per-particle adaptive Dormand-Prince (extension): every particle reaches t_end within the
+    tolerance, and slow particles take fewer, longer steps than the global step imposes."""
+    e_pp, sweeps, accepted = _rotation_radii(True)
+    e_gl, steps, _ = _rotation_radii(False)
+    assert e_pp <= 1e-6 and e_gl <= 1e-6, (e_pp, e_gl)
+    assert accepted < 24 * steps, (accepted, steps)
+    assert sweeps >= steps  # the fastest particle needs as many steps as the global scheme
