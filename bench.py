@@ -195,20 +195,24 @@ def run_serving(njobs, workers=8, budget=150e9):
                         "FP32 evaluation; latency from submission"}
 
 
-def run_uneven(rk4_steps=3, dopri_steps=5):
+def run_uneven(rk4_steps=3, dopri_steps=5, t_end=0.1, pp_budget_s=90.0):
     """The uneven configuration: 1M points (90 % from 8 Gaussians of widths 0.02-0.2, 10 % uniform),
     ABC flow, 8M particles from the same mixture, Wendland C2 on a uniform 160^3 PU mesh (largest
     patch 1,713 points, 2.3M non-empty patches).  Set-up time, then FP32-evaluation RK4 steps at
-    the CFL step and Dormand-Prince steps (rtol 1e-6, atol 1e-9, global adapted step) over an
-    interval of about `dopri_steps` of the step adapted by a first call."""
+    the CFL step, Dormand-Prince steps (rtol 1e-6, atol 1e-9, the reference's global adapted step)
+    over an interval of about `dopri_steps` of the step adapted by a first call, and per-particle
+    adaptive Dormand-Prince (same tolerances) run towards t_end in intervals of t_end / 10 until
+    t_end or pp_budget_s of wall time: accepted particle steps per second, sweeps, time reached."""
     import lagrbf_gb300 as L
     from lagrbf_gb300 import workloads as W
     xd, fd, xp, opts = W.config_uneven_3d()
     out = {"workload": "uneven: 1M-point Gaussian mixture + 10% uniform, ABC flow, 160^3 PU, Wendland C2, "
                        "8M particles from the mixture, FP32 evaluation"}
-    for scheme, name in ((2, "rk4"), (3, "dopri")):
+    for scheme, name in ((2, "rk4"), (3, "dopri"), (3, "dopri_per_particle")):
+        pp = name == "dopri_per_particle"
         c = L.LagRBFCtx(**opts, advection=True, advection_scheme=scheme, advection_cfl=0.3, solve_method=1,
-                        eval_precision="fp32", dt=DT, petsc_options={"dopri_rtol": 1e-6, "dopri_atol": 1e-9})
+                        eval_precision="fp32", dt=DT, petsc_options={"dopri_rtol": 1e-6, "dopri_atol": 1e-9,
+                                                                      "dopri_per_particle": pp})
         c.synchronize()
         ts = time.perf_counter()
         c.fill_data(xd, fd); c.fill_points(xp); c.interpolate_c(); c.synchronize()
@@ -216,6 +220,21 @@ def run_uneven(rk4_steps=3, dopri_steps=5):
             st = c.stats()
             out.update(setup_s=time.perf_counter() - ts, max_patch=st["max_patch"],
                        patches_factored=st["patches_factored"])
+        if pp:
+            c.reset_stats()
+            ts = time.perf_counter()
+            t = 0.0
+            while t < t_end - 1e-15 and time.perf_counter() - ts < pp_budget_s:
+                c.advect_resident(t, t + t_end / 10)
+                t += t_end / 10
+            c.synchronize()
+            el = time.perf_counter() - ts
+            st = c.stats()
+            out[name] = {"value": st["particle_steps"] / el, "unit": "accepted particle-steps/s",
+                         "sweeps": st["steps"], "accepted_particle_steps": st["particle_steps"],
+                         "t_reached": t, "t_end": t_end, "seconds": el, "np_alive": st["np_alive"]}
+            del c
+            continue
         t = 0.0
         c.advect_resident(t, t + 1e-5); t += 1e-5  # warm-up (and the first adapted step for DOPRI)
         c.synchronize()
