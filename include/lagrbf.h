@@ -93,7 +93,9 @@ LAGRBF_EXPORT void lagrbf_interpolate_driver(int32_t ndata_local, double *data_c
    default fp64), use_cuda_graph (bool, default true), cuda_device (int), output_direct (bool,
    default true: when the device accesses pageable host memory, lagrbf_output's particle rows are
    written by the GPU straight into the caller's arrays and lagrbf_fill_swarm's data arrays are
-   read by it directly).  Arrays are comma separated. */
+   read by it directly), dopri_per_particle (bool, default false: per-particle adaptive
+   Dormand-Prince, an extension), setup_all_patches (bool, default false: set up every patch, not
+   only those of cells holding particles).  Arrays are comma separated. */
 LAGRBF_EXPORT int lagrbf_options_set_value(const char *name, const char *value);
 LAGRBF_EXPORT int lagrbf_options_clear(void);
 LAGRBF_EXPORT int lagrbf_options_insert_file(const char *path);
@@ -150,6 +152,16 @@ LAGRBF_EXPORT double lagrbf_gpu_fp32_peak_tflops(void);
    patches not factored while on) and summary[3] = {max, median, count} of the non-zero ones. */
 LAGRBF_EXPORT int lagrbf_gpu_set_condition_estimates(void *ctx, int on);
 LAGRBF_EXPORT int lagrbf_gpu_get_condition(void *ctx, double *kappa, double *summary);
+/* Coupling of sharded runs (one process and GPU per rank, each holding the whole dataset and a pid
+   range of the particles): fn(vals, n, user) must replace vals[0..n) by their element-wise maximum
+   over the ranks (e.g. an MPI_Allreduce with MPI_MAX) and return 0.  Each internal step of the
+   advection loops passes {-(the local CFL step), the local Dormand-Prince error}, so every rank takes
+   the reference's global step (advection.c:466, dormand_prince.c:93) for any outer interval, and
+   once before the first step.  Per-particle Dormand-Prince needs no coupling and does not call it.
+   The reference sets up only the patches of cells holding particles (partition.c:452-469), which
+   depends on where every rank's particles are: sharded runs equal the single-rank run bit for bit
+   when both use the option setup_all_patches (every patch set up).  NULL removes it. */
+LAGRBF_EXPORT int lagrbf_gpu_set_step_reduce(void *ctx, int (*fn)(double *vals, int32_t n, void *user), void *user);
 /* Test hook of the evaluation kernel's bounded waits: poll_limit (> 0) replaces the default number
    of polls after which a wait on a staging copy gives up (0 restores it); with withhold_copies the
    kernel arms its staging barriers but issues no copy, so every wait runs out and the call returns

@@ -38,6 +38,10 @@ VELOCITY_FN_BATCH = ctypes.CFUNCTYPE(ctypes.c_int, PetscInt, PetscInt, ctypes.PO
                                      ctypes.POINTER(PetscReal), ctypes.c_void_p)
 
 
+# int fn(double *vals, int32 n, void *user): element-wise max of vals over the ranks, in place
+STEP_REDUCE = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.POINTER(ctypes.c_double), ctypes.c_int32, ctypes.c_void_p)
+
+
 class Stats(ctypes.Structure):
     _fields_ = [
         ("launches", ctypes.c_int64), ("eval_launches", ctypes.c_int64), ("eval_flops", ctypes.c_double),
@@ -93,6 +97,7 @@ def register_functions(clib):
     reg("lagrbf_options_get_value", ctypes.c_int, [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_int32])
     # GPU extension
     reg("lagrbf_gpu_set_profiling", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int])
+    reg("lagrbf_gpu_set_step_reduce", ctypes.c_int, [ctypes.c_void_p, STEP_REDUCE, ctypes.c_void_p])
     reg("lagrbf_gpu_set_condition_estimates", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int])
     reg("lagrbf_gpu_get_condition", ctypes.c_int, [ctypes.c_void_p, real_pn, real_pn])
     reg("lagrbf_gpu_test_eval_wait", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32])

@@ -10,7 +10,7 @@ import os
 
 import numpy as np
 
-from ._lib import load_cfuncs, last_error, Stats, VELOCITY_FN, VELOCITY_FN_BATCH
+from ._lib import load_cfuncs, last_error, Stats, STEP_REDUCE, VELOCITY_FN, VELOCITY_FN_BATCH
 
 
 def _fmt(v):
@@ -234,6 +234,25 @@ class LagRBFCtx:
 
     def set_profiling(self, on):
         self._check(self._cf["lagrbf_gpu_set_profiling"](self.ctx, int(bool(on))), "lagrbf_gpu_set_profiling")
+
+    def set_step_reduce(self, fn):
+        """Coupling of sharded runs (lagrbf_gpu_set_step_reduce): fn(vals) replaces the numpy array
+        vals by its element-wise maximum over the ranks; None removes it."""
+        if fn is None:
+            self._step_reduce = None
+            self._check(self._cf["lagrbf_gpu_set_step_reduce"](self.ctx, STEP_REDUCE(), None),
+                        "lagrbf_gpu_set_step_reduce")
+            return
+
+        def cb(ptr, n, user):
+            try:
+                fn(np.ctypeslib.as_array(ptr, shape=(n,)))
+                return 0
+            except Exception:  # an error code, never an exception through the C frame
+                return 1
+        self._step_reduce = STEP_REDUCE(cb)
+        self._check(self._cf["lagrbf_gpu_set_step_reduce"](self.ctx, self._step_reduce, None),
+                    "lagrbf_gpu_set_step_reduce")
 
     def set_condition_estimates(self, on):
         """Per-patch 1-norm condition estimates at every factorisation (lagrbf_gpu_set_condition_estimates)."""

@@ -400,11 +400,22 @@ __global__ void k_compact(int nnodes, int *__restrict__ need, int *__restrict__ 
   }
 }
 
+/* Option setup_all_patches: every patch not yet set up or solved is queued. */
+__global__ void k_mark_all(int nnodes, const int *__restrict__ setup, const int *__restrict__ solved,
+                           int *__restrict__ need)
+{
+  int node = blockIdx.x * blockDim.x + threadIdx.x;
+  if (node < nnodes && (!setup[node] || !solved[node])) need[node] = 1;
+}
+
 extern "C" int lgb_op_mark_patches(lgb_dev *d, void *stream)
 {
   cudaStream_t s = (cudaStream_t)stream;
   cudaMemsetAsync(&d->ctrl->nwork, 0, sizeof(int), s);
-  if (d->np > 0) {
+  if (d->setup_all) {
+    k_mark_all<<<lgb_cdiv(d->g.nnodes, 256), 256, 0, s>>>(d->g.nnodes, d->setup, d->solved, d->need);
+    lgb_count_launch(1);
+  } else if (d->np > 0) {
     k_mark<<<lgb_cdiv(d->np, 256), 256, 0, s>>>(d->g, d->np, d->cell_p, d->alive, d->setup, d->solved, d->need);
     lgb_count_launch(1);
   }

@@ -251,6 +251,9 @@ typedef struct {
   vfn_t vfn;
   vfnb_t vfnb;
   void *vuser;
+  /* coupling of sharded runs: element-wise max over the ranks of {-(CFL step), DOPRI error} */
+  int (*reduce)(double *, int32_t, void *);
+  void *ruser;
   /* graph of one internal step */
   cudaGraphExec_t graph;
   int graph_valid, graph_mode; /* graph_mode: 1 when the captured step is analytical */
@@ -467,6 +470,8 @@ static int read_options(lgb_ctx *c)
   opt_real("dopri_rtol", &c->dopri[4]);
   d->dopri_pp = 0;
   opt_bool("dopri_per_particle", &d->dopri_pp);
+  d->setup_all = 0;
+  opt_bool("setup_all_patches", &d->setup_all);
   d->prec = LGB_PREC_FP64;
   if (opt_str("eval_precision", buf, sizeof(buf))) {
     if (strcmp(buf, "fp32") == 0) d->prec = LGB_PREC_FP32;
@@ -1073,7 +1078,7 @@ static int step_sequence(lgb_ctx *c, int analytical)
       TRY(eval_velocity(c, analytical));
     }
     OP(lgb_op_dopri_error(d, s));
-    OP(lgb_op_ctrl(d, LGB_CTRL_DOPRI_DT, s));
+    if (!c->reduce) OP(lgb_op_ctrl(d, LGB_CTRL_DOPRI_DT, s)); /* coupled runs: after the reduction */
     break;
   default:
     return set_error(LAGRBF_ERR_ARG_OUTOFRANGE, "unknown scheme");
@@ -1089,6 +1094,38 @@ static int step_sequence(lgb_ctx *c, int analytical)
     OP(lgb_op_count_alive(d, s));
   }
   OP(lgb_op_ctrl(d, pp ? LGB_CTRL_END_SWEEP : LGB_CTRL_END_STEP, s));
+  return 0;
+}
+
+/* Coupled (sharded) runs: the step's local CFL step (from the largest |v|^2, as k_ctrl computes it)
+   and DOPRI error are reduced over the ranks by the registered function, written back, and the
+   DOPRI step update runs on the global error (the reference's MPI_Allreduce at advection.c:466 and
+   dormand_prince.c:93).  hctrl holds the control block read after the step. */
+static int couple_ranks(lgb_ctx *c, int dopri_update)
+{
+  lgb_ctrl *h = c->hctrl;
+  double v[2], dt_cfl = DBL_MAX;
+  int rc;
+  if (h->n2max_bits) {
+    double n2;
+    unsigned long long b = h->n2max_bits - 1ull;
+    memcpy(&n2, &b, sizeof n2);
+    dt_cfl = h->cfl_fac * h->cfl_radius / (sqrt(n2) + 1e-16);
+  }
+  v[0] = -dt_cfl;
+  v[1] = -DBL_MAX;
+  if (dopri_update && h->any_alive) memcpy(&v[1], &h->maxerr_bits, sizeof(double));
+  if ((rc = c->reduce(v, 2, c->ruser)))
+    return set_error(LAGRBF_ERR_PLIB, "step reduction callback failed (%d)", rc);
+  h->dt_cfl_ext = (-v[0] < DBL_MAX) ? -v[0] : 0.0;
+  if (dopri_update) {
+    h->any_alive = v[1] >= 0.0;
+    if (h->any_alive) memcpy(&h->maxerr_bits, &v[1], sizeof(double));
+  }
+  CU(cudaMemcpyAsync(c->d.ctrl, h, sizeof(lgb_ctrl), cudaMemcpyHostToDevice, c->stream));
+  if (dopri_update) OP(lgb_op_ctrl(&c->d, LGB_CTRL_DOPRI_DT, c->stream));
+  CU(cudaMemcpyAsync(h, c->d.ctrl, sizeof(lgb_ctrl), cudaMemcpyDeviceToHost, c->stream));
+  CU(cudaStreamSynchronize(c->stream));
   return 0;
 }
 
@@ -1144,7 +1181,9 @@ static int run_step(lgb_ctx *c, int analytical)
   CU(cudaMemcpyAsync(c->hctrl, c->d.ctrl, sizeof(lgb_ctrl), cudaMemcpyDeviceToHost, c->stream));
   CU(cudaStreamSynchronize(c->stream));
   if (c->hctrl->factor_error) return check_factor_error(c);
-  return check_eval_error(c);
+  TRY(check_eval_error(c));
+  if (c->reduce && !(c->scheme == LGB_DOPRI && c->d.dopri_pp)) TRY(couple_ranks(c, c->scheme == LGB_DOPRI));
+  return 0;
 }
 
 static int advection_loop(lgb_ctx *c, double t, double t_next, int analytical, int keep)
@@ -1173,6 +1212,11 @@ static int advection_loop(lgb_ctx *c, double t, double t_next, int analytical, i
   }
   if (c->scheme == LGB_DOPRI && d->dopri_pp) OP(lgb_op_pp_init(d, t, c->stream));
   CU(cudaStreamSynchronize(c->stream));
+  if (c->reduce && !(c->scheme == LGB_DOPRI && d->dopri_pp)) {
+    CU(cudaMemcpyAsync(c->hctrl, d->ctrl, sizeof(lgb_ctrl), cudaMemcpyDeviceToHost, c->stream));
+    CU(cudaStreamSynchronize(c->stream));
+    TRY(couple_ranks(c, 0)); /* the first step's CFL step over all ranks */
+  }
   while (t < t_next) {
     TRY(run_step(c, analytical));
     t = c->hctrl->t;
@@ -1466,6 +1510,21 @@ LAGRBF_EXPORT int lagrbf_gpu_set_precision(void *ctx, int fp32)
   if (!c) return set_error(LAGRBF_ERR_ARG_NULL, "context is NULL");
   CU(cudaStreamSynchronize(c->stream));
   c->d.prec = fp32 ? LGB_PREC_FP32 : LGB_PREC_FP64;
+  invalidate_graph(c);
+  return 0;
+}
+
+LAGRBF_EXPORT int lagrbf_gpu_set_step_reduce(void *ctx, int (*fn)(double *, int32_t, void *), void *user)
+{
+  lgb_ctx *c = (lgb_ctx *)ctx;
+  if (!c) return set_error(LAGRBF_ERR_ARG_NULL, "context is NULL");
+  CU(cudaStreamSynchronize(c->stream));
+  c->reduce = fn;
+  c->ruser = user;
+  if (!fn) {
+    c->hctrl->dt_cfl_ext = 0.0;
+    CU(cudaMemcpy(&c->d.ctrl->dt_cfl_ext, &c->hctrl->dt_cfl_ext, sizeof(double), cudaMemcpyHostToDevice));
+  }
   invalidate_graph(c);
   return 0;
 }

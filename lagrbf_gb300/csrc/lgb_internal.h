@@ -103,6 +103,7 @@ typedef struct {
   double factor_flops;
   int eval_error;      /* a bounded wait of the evaluation kernel gave up */
   int pp_left;         /* per-particle Dormand-Prince: particles still short of t_next   */
+  double dt_cfl_ext;   /* > 0: the CFL step agreed over ranks (replaces the local one)     */
   double pp_hmin;      /* per-particle Dormand-Prince: steps below this are accepted      */
 } lgb_ctrl;
 
@@ -132,6 +133,8 @@ typedef struct {
   /* per-particle adaptive Dormand-Prince (option dopri_per_particle): time reached, next step, step
      of the current sweep, and whether the particle takes part in the sweep */
   int dopri_pp;
+  int setup_all;       /* option setup_all_patches: every patch is set up, not only those of cells
+                          holding particles */
   double *tp, *hp, *hcur;
   int *active;
   long long ws_stride;

@@ -460,6 +460,7 @@ __global__ void k_ctrl(lgb_ctrl *c, int what)
       const double n2 = __longlong_as_double((long long)(c->n2max_bits - 1ull));
       dt_cfl = c->cfl_fac * c->cfl_radius / (sqrt(n2) + 1e-16);
     }
+    if (c->dt_cfl_ext > 0.0) dt_cfl = c->dt_cfl_ext;
     double dt = (c->scheme == LGB_DOPRI) ? ((c->dt_adv < dt_cfl) ? c->dt_adv : dt_cfl) : dt_cfl;
     if (c->t + dt > c->t_next) dt = c->t_next - c->t;
     c->dt = dt;

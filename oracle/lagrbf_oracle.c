@@ -624,6 +624,8 @@ struct orc_ctx {
   orc_velocity_fn vfn;
   orc_velocity_batch_fn vfn_batch;
   void *vuser;
+  orc_step_reduce_fn reduce;
+  void *ruser;
 };
 
 static void *xrealloc(void *p, size_t n) { void *q = realloc(p, n ? n : 1); return q; }
@@ -775,50 +777,62 @@ int orc_fill_swarm(orc_ctx *c, int is_data, int n, const double *coords, const d
 }
 
 /* Lazy patch set-up and solve (LagRBF_PartitionsSetUp, partition.c:417-478). */
+/* LagRBF_PartitionsSetUp for one patch node (partition.c:417-478): set up (membership, assembly,
+   factor) and solve when not done yet. */
+static int setup_node(orc_ctx *c, int node)
+{
+  int F = c->cfg.nfields;
+  if (!c->patch_setup[node]) {
+    /* PartitionSetUp_SinglePartition: membership from the current data-swarm sort */
+    long len = orc_patch_csr(&c->pu, c->cell_start, c->cell_pts, NULL, NULL);
+    int m, info;
+    if (len != c->patch_len || !c->patch_pts) {
+      c->patch_pts = (int *)xrealloc(c->patch_pts, sizeof(int) * (size_t)(len ? len : 1));
+      c->patch_len = len;
+    }
+    orc_patch_csr(&c->pu, c->cell_start, c->cell_pts, c->patch_start, c->patch_pts);
+    m = c->patch_start[node + 1] - c->patch_start[node];
+    c->patch_idx[node] = (int *)malloc(sizeof(int) * (size_t)(m ? m : 1));
+    if (m) memcpy(c->patch_idx[node], &c->patch_pts[c->patch_start[node]], sizeof(int) * (size_t)m);
+    c->patch_m[node] = m;
+    c->coeffs[node] = (double *)calloc((size_t)(m ? m : 1) * (F ? F : 1), sizeof(double));
+    if (m) {
+      double *A = (double *)malloc(sizeof(double) * (size_t)m * m);
+      assemble(&c->pu, c->cfg.kernel, m, c->patch_idx[node], c->xd, A);
+      info = cholesky(m, A);
+      if (info) { free(A); return ORC_ERR_MAT_CH_ZRPVT; }
+      c->factor[node] = A;
+    }
+    c->patch_setup[node] = 1;
+  }
+  if (!c->patch_solved[node]) {
+    /* PartitionSolveInterpolationCoefficients_SinglePartition, partition_solve.c:97-113 */
+    int m = c->patch_m[node];
+    if (m > 0) {
+      patch_rhs_solve(m, c->patch_idx[node], c->factor[node], F, c->fd, c->coeffs[node]);
+      if (c->cfg.solve_method == ORC_A_KSP_ASMB || c->cfg.solve_method == ORC_A_FACTOR) {
+        /* the assembled/factored matrix is released after the solve; A_FACTOR reloads its
+           factor from disk on the next solve, which keeping it here reproduces */
+        if (c->cfg.solve_method == ORC_A_KSP_ASMB) { free(c->factor[node]); c->factor[node] = NULL; }
+      }
+      c->patch_solved[node] = 1;
+    }
+  }
+  return 0;
+}
+
 static int partitions_setup(orc_ctx *c)
 {
-  int p, k, F = c->cfg.nfields;
+  int p, k, node, err;
+  if (c->cfg.setup_all) { /* extension: every patch, independent of where the particles are */
+    for (node = 0; node < c->pu.nnodes; node++)
+      if ((err = setup_node(c, node))) return err;
+    return 0;
+  }
   for (p = 0; p < c->np; p++) {
     if (!c->alive[p] || c->cell_p[p] < 0) continue;
-    for (k = 0; k < c->pu.nen; k++) {
-      int node = orc_cell_corner(&c->pu, c->cell_p[p], k);
-      if (!c->patch_setup[node]) {
-        /* PartitionSetUp_SinglePartition: membership from the current data-swarm sort */
-        long len = orc_patch_csr(&c->pu, c->cell_start, c->cell_pts, NULL, NULL);
-        int m, info;
-        if (len != c->patch_len || !c->patch_pts) {
-          c->patch_pts = (int *)xrealloc(c->patch_pts, sizeof(int) * (size_t)(len ? len : 1));
-          c->patch_len = len;
-        }
-        orc_patch_csr(&c->pu, c->cell_start, c->cell_pts, c->patch_start, c->patch_pts);
-        m = c->patch_start[node + 1] - c->patch_start[node];
-        c->patch_idx[node] = (int *)malloc(sizeof(int) * (size_t)(m ? m : 1));
-        if (m) memcpy(c->patch_idx[node], &c->patch_pts[c->patch_start[node]], sizeof(int) * (size_t)m);
-        c->patch_m[node] = m;
-        c->coeffs[node] = (double *)calloc((size_t)(m ? m : 1) * (F ? F : 1), sizeof(double));
-        if (m) {
-          double *A = (double *)malloc(sizeof(double) * (size_t)m * m);
-          assemble(&c->pu, c->cfg.kernel, m, c->patch_idx[node], c->xd, A);
-          info = cholesky(m, A);
-          if (info) { free(A); return ORC_ERR_MAT_CH_ZRPVT; }
-          c->factor[node] = A;
-        }
-        c->patch_setup[node] = 1;
-      }
-      if (!c->patch_solved[node]) {
-        /* PartitionSolveInterpolationCoefficients_SinglePartition, partition_solve.c:97-113 */
-        int m = c->patch_m[node];
-        if (m > 0) {
-          patch_rhs_solve(m, c->patch_idx[node], c->factor[node], F, c->fd, c->coeffs[node]);
-          if (c->cfg.solve_method == ORC_A_KSP_ASMB || c->cfg.solve_method == ORC_A_FACTOR) {
-            /* the assembled/factored matrix is released after the solve; A_FACTOR reloads its
-               factor from disk on the next solve, which keeping it here reproduces */
-            if (c->cfg.solve_method == ORC_A_KSP_ASMB) { free(c->factor[node]); c->factor[node] = NULL; }
-          }
-          c->patch_solved[node] = 1;
-        }
-      }
-    }
+    for (k = 0; k < c->pu.nen; k++)
+      if ((err = setup_node(c, orc_cell_corner(&c->pu, c->cell_p[p], k)))) return err;
   }
   return 0;
 }
@@ -1082,6 +1096,11 @@ static int dopri(orc_ctx *c)
     E = sqrt(1.0 / dim * E);
     max_err = ORC_MAX(max_err, E);
   }
+  if (c->reduce) { /* global maximum of the error over the ranks (dormand_prince.c:93) */
+    double v[2] = {-ORC_MAX_REAL, max_err};
+    if ((err = c->reduce(v, 2, c->ruser))) return err;
+    max_err = v[1];
+  }
   c->dopri_error = max_err;
   migrate_and_weights(c);
   fac = c->cfg.dopri_dt_fac;
@@ -1219,8 +1238,20 @@ static int advection_loop(orc_ctx *c, double t, double t_next, int interpolated,
     double dt;
     if (c->cfg.scheme == ORC_DOPRI) {
       double dt_cfl = cfl_dt(c);
+      if (c->reduce) { /* global minimum of the CFL step over the ranks (advection.c:466) */
+        double v[2] = {-dt_cfl, -ORC_MAX_REAL};
+        if ((err = c->reduce(v, 2, c->ruser))) return err;
+        dt_cfl = -v[0];
+      }
       dt = ORC_MIN(c->dt, dt_cfl);
-    } else dt = cfl_dt(c);
+    } else {
+      dt = cfl_dt(c);
+      if (c->reduce) {
+        double v[2] = {-dt, -ORC_MAX_REAL};
+        if ((err = c->reduce(v, 2, c->ruser))) return err;
+        dt = -v[0];
+      }
+    }
     if (t + dt > t_next) dt = t_next - t;
     c->dt = dt;
     if ((err = advect_swarm(c))) return err;
@@ -1256,6 +1287,7 @@ int orc_advect_analytical(orc_ctx *c, double t, double t_next)
 
 int orc_set_velocity_fn(orc_ctx *c, orc_velocity_fn fn, void *user) { c->vfn = fn; c->vuser = user; return 0; }
 int orc_set_velocity_batch_fn(orc_ctx *c, orc_velocity_batch_fn fn, void *user) { c->vfn_batch = fn; c->vuser = user; return 0; }
+int orc_set_step_reduce(orc_ctx *c, orc_step_reduce_fn fn, void *user) { c->reduce = fn; c->ruser = user; return 0; }
 
 int orc_get_counts(orc_ctx *c, int *nd, int *np_alive, int *npatch_setup, int *nsteps)
 {

@@ -44,6 +44,8 @@ typedef struct {
   double dopri_dt_fac, dopri_dt_fac_min, dopri_dt_fac_max, dopri_atol, dopri_rtol;
   int    dopri_per_particle; /* extension: per-particle adaptive Dormand-Prince (0: the reference's
                                 single global step, always accepted)                              */
+  int    setup_all;          /* extension: set up every patch, not only those of cells holding
+                                particles (the lazy set-up of partition.c:452-469)               */
 } orc_config;
 
 /* Defaults of LagRBFCtxCreate (src/lagrangian_rbf.c:36-73), AdvectionCtxCreate
@@ -118,6 +120,12 @@ int      orc_advect_interpolate(orc_ctx *ctx, double t, double t_next);      /* 
 int      orc_advect_analytical(orc_ctx *ctx, double t, double t_next);       /* time_loop.c:176-221 */
 int      orc_set_velocity_fn(orc_ctx *ctx, orc_velocity_fn fn, void *user);
 int      orc_set_velocity_batch_fn(orc_ctx *ctx, orc_velocity_batch_fn fn, void *user);
+/* Coupling of sharded runs (the reference's MPI_Allreduce at advection.c:466 and
+   dormand_prince.c:93): fn replaces vals[0..n) by their element-wise maximum over the ranks.  Each
+   internal step the oracle passes {-(CFL step), DOPRI error} (the negated step, so that the maximum
+   is the global minimum step). */
+typedef int (*orc_step_reduce_fn)(double *vals, int32_t n, void *user);
+int      orc_set_step_reduce(orc_ctx *ctx, orc_step_reduce_fn fn, void *user);
 /* Inspection for tests. */
 int      orc_get_counts(orc_ctx *ctx, int *nd, int *np_alive, int *npatch_setup, int *nsteps);
 double   orc_get_dt(orc_ctx *ctx);

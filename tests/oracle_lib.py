@@ -23,6 +23,7 @@ class OrcConfig(ctypes.Structure):
         ("rmin", ctypes.c_double), ("rmax", ctypes.c_double), ("dopri_dt_fac", ctypes.c_double),
         ("dopri_dt_fac_min", ctypes.c_double), ("dopri_dt_fac_max", ctypes.c_double),
         ("dopri_atol", ctypes.c_double), ("dopri_rtol", ctypes.c_double), ("dopri_per_particle", ctypes.c_int),
+        ("setup_all", ctypes.c_int),
     ]
 
 
@@ -34,6 +35,7 @@ class OrcPU(ctypes.Structure):
     ]
 
 
+STEP_REDUCE = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.POINTER(ctypes.c_double), ctypes.c_int32, ctypes.c_void_p)
 VFN_BATCH = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_int32, ctypes.c_int32, ctypes.POINTER(ctypes.c_double),
                              ctypes.POINTER(ctypes.c_double), ctypes.c_void_p)
 
@@ -81,6 +83,7 @@ def lib():
         L.orc_advect_analytical.argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.c_double]
         L.orc_set_velocity_batch_fn.argtypes = [ctypes.c_void_p, VFN_BATCH, ctypes.c_void_p]
         L.orc_get_counts.argtypes = [ctypes.c_void_p] + [ctypes.POINTER(ctypes.c_int)] * 4
+        L.orc_set_step_reduce.argtypes = [ctypes.c_void_p, STEP_REDUCE, ctypes.c_void_p]
         L.orc_get_accepted.restype = ctypes.c_longlong
         L.orc_get_accepted.argtypes = [ctypes.c_void_p]
         L.orc_get_dt.restype = ctypes.c_double
@@ -117,7 +120,8 @@ def lib():
 
 def make_config(dim, npartitions, nfields, kernel=2, overlap=1.0, shape_factor=1.0, minCoords=None,
                 maxCoords=None, solve_method=2, advection=False, advection_scheme=2, advection_cfl=0.3,
-                dt=1e-4, rmin=0.0, rmax=1e132, dopri_per_particle=False, dopri_rtol=None, dopri_atol=None, **_):
+                dt=1e-4, rmin=0.0, rmax=1e132, dopri_per_particle=False, dopri_rtol=None, dopri_atol=None,
+                setup_all_patches=False, **_):
     """Config with the lagrbfpy keyword defaults (context.py:113-201)."""
     c = OrcConfig()
     lib().orc_config_default(ctypes.byref(c))
@@ -129,6 +133,7 @@ def make_config(dim, npartitions, nfields, kernel=2, overlap=1.0, shape_factor=1
     c.overlap, c.shape_factor, c.kernel, c.solve_method, c.nfields = overlap, shape_factor, kernel, solve_method, nfields
     c.advection, c.scheme, c.cfl_fac, c.dt, c.rmin, c.rmax = int(advection), advection_scheme, advection_cfl, dt, rmin, rmax
     c.dopri_per_particle = int(bool(dopri_per_particle))
+    c.setup_all = int(bool(setup_all_patches))
     if dopri_rtol is not None:
         c.dopri_rtol = dopri_rtol
     if dopri_atol is not None:
@@ -185,6 +190,15 @@ class Oracle:
         cb = VFN_BATCH(fn)
         self._keep.append(cb)
         return lib().orc_set_velocity_batch_fn(self.h, cb, None)
+
+    def set_step_reduce(self, fn):
+        """fn(vals: numpy view of n doubles) reduces them in place (element-wise max over ranks)."""
+        def cb(ptr, n, user):
+            fn(np.ctypeslib.as_array(ptr, shape=(n,)))
+            return 0
+        c = STEP_REDUCE(cb)
+        self._keep.append(c)
+        return lib().orc_set_step_reduce(self.h, c, None)
 
     def counts(self):
         v = [ctypes.c_int() for _ in range(4)]

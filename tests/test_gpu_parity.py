@@ -589,3 +589,46 @@ def _rot3(n, dim, x, v):
         v[dim * p + 1] = 2.0 * (x[dim * p] - 0.5)
         v[dim * p + 2] = 0.0
     return 0
+
+
+@pytest.mark.parametrize("scheme", [2, 3])
+def test_step_reduce_coupling_matches_oracle(scheme):
+    """The coupling of sharded runs (lagrbf_gpu_set_step_reduce), driven by a stand-in for the other
+    ranks: it caps the CFL step at 1.5e-3 and raises the Dormand-Prince error to at least 0.5, as a
+    rank holding faster particles would.  The GPU and the oracle with the same reduction take the
+    same steps; the callback sees every internal step plus the first one's CFL step."""
+    xd, fd, xp, opts = small_3d(np_=1000)
+    adv = dict(advection=True, advection_scheme=scheme, advection_cfl=0.3, dt=1e-3, solve_method=1,
+               setup_all_patches=True)
+    calls = []
+
+    def other_ranks(v):
+        calls.append(v.copy())
+        v[0] = max(v[0], -1.5e-3)
+        v[1] = max(v[1], 0.5)
+
+    c = gpu_ctx(opts, **adv)
+    c.set_step_reduce(other_ranks)
+    o = Oracle(**opts, **adv)
+    assert o.set_step_reduce(other_ranks) == 0
+    c.fill_points(xp)
+    assert o.fill(False, xp) == 0
+    n_oracle = len(calls)
+    t, dt = 0.0, 1e-2
+    for _ in range(2):
+        c.fill_data(xd, fd); c.interpolate_c()
+        assert o.fill(True, xd, fd) == 0 and o.interpolate() == 0
+        n0 = len(calls)
+        c.advect_interpolate_c(t, t + dt)
+        n_gpu = len(calls) - n0
+        n1 = len(calls)
+        assert o.advect(t, t + dt) == 0
+        assert n_gpu >= 2 and len(calls) - n1 >= 1
+        t += dt
+    x1, f1, p1 = gpu_output(c, len(xp), 3)
+    x2, f2, p2 = o.output(len(xp))
+    assert np.array_equal(p1, p2)
+    assert c.stats()["steps"] == o.counts()[3] >= 14
+    assert np.abs(x1 - x2).max() <= 1e-12
+    assert relerr(f1, f2) <= TOL64
+    del n_oracle
