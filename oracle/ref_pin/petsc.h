@@ -1,7 +1,8 @@
 /*
  * petsc.h -- minimal stand-in for the PETSc API surface used by LagRBF's hot-loop translation
  * units, so that those units compile unmodified, in place, into a test-only library that checks
- * the oracle (TEST INFRASTRUCTURE ONLY: never linked into liblagrbf.so).
+ * the oracle (TEST INFRASTRUCTURE ONLY: never linked into liblagrbf.so).  The GPU plug-ins of
+ * lagrbf_gb300/adapters/petsc are compile-checked against the reference headers with it too.
  *
  * Types follow the reference's PETSc configuration (32-bit indices, double precision):
  * PetscInt = int32_t, PetscReal = PetscScalar = double.  DM / Mat / Vec are handles to the small
@@ -85,5 +86,8 @@ PetscErrorCode DMSwarmCellDMGetCoordinateFields(DMSwarmCellDM celldm, PetscInt *
 PetscErrorCode DMSwarmCellDMGetCellID(DMSwarmCellDM celldm, const char **name);
 PetscErrorCode DMSwarmGetField(DM sw, const char *name, PetscInt *bs, PetscDataType *type, void **data);
 PetscErrorCode DMSwarmRestoreField(DM sw, const char *name, PetscInt *bs, PetscDataType *type, void **data);
+/* declared for the compile check of the GPU plug-ins (lagrbf_gb300/adapters/petsc); not defined */
+#define DMSwarmField_pid "DMSwarm_pid"
+PetscErrorCode DMSwarmRemovePointAtIndex(DM sw, PetscInt idx);
 
 #endif
