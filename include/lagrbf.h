@@ -125,6 +125,8 @@ typedef struct {
   int32_t records;            /* 1 when precomputed record blocks are streamed by TMA         */
   double  kappa_max;          /* largest / median 1-norm condition estimate of the patches     */
   double  kappa_median;       /* factored with lagrbf_gpu_set_condition_estimates on (else 0)  */
+  int32_t device_loop;        /* 1 when advection intervals run as one graph launch with the
+                                 internal steps looping on the device (conditional while node)  */
 } lagrbf_stats_t;
 
 /* The interpolated advection loop of lagrbf_advect_interpolate over [time, time_next] without its

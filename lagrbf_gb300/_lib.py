@@ -50,7 +50,7 @@ class Stats(ctypes.Structure):
         ("factor_flops", ctypes.c_double), ("np_alive", ctypes.c_int32), ("nd", ctypes.c_int32),
         ("max_patch", ctypes.c_int32), ("npatch_setup", ctypes.c_int32), ("dt", ctypes.c_double),
         ("chunk_cap", ctypes.c_int32), ("records", ctypes.c_int32), ("kappa_max", ctypes.c_double),
-        ("kappa_median", ctypes.c_double),
+        ("kappa_median", ctypes.c_double), ("device_loop", ctypes.c_int32),
     ]
 
     def as_dict(self):

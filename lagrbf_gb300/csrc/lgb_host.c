@@ -258,6 +258,10 @@ typedef struct {
   cudaGraphExec_t graph;
   int graph_valid, graph_mode; /* graph_mode: 1 when the captured step is analytical */
   long long graph_launches, graph_eval_launches;
+  /* the step inside a device-side while loop: one launch advances a whole advection interval */
+  cudaGraphExec_t wgraph;
+  int wgraph_valid, wgraph_mode, wgraph_failed;
+  long long wgraph_launches, wgraph_eval_launches;
   /* pinned control copy */
   lgb_ctrl *hctrl;
   /* profiling */
@@ -283,6 +287,8 @@ static void invalidate_graph(lgb_ctx *c)
 {
   if (c->graph_valid) cudaGraphExecDestroy(c->graph);
   c->graph_valid = 0;
+  if (c->wgraph_valid) cudaGraphExecDestroy(c->wgraph);
+  c->wgraph_valid = 0;
 }
 
 static void free_data(lgb_dev *d)
@@ -1186,6 +1192,70 @@ static int run_step(lgb_ctx *c, int analytical)
   return 0;
 }
 
+static int step_sequence(lgb_ctx *c, int analytical);
+
+/* The internal steps of one advection interval as one graph launch: the step is the body of a
+   conditional while node whose condition kernel continues while t < t_next (and no error flag is
+   set, and at most loop_cap steps), so the host neither launches nor synchronises per step.
+   Returns 1 when the interval was run this way, 0 when the caller must step from the host (coupled
+   runs, host callbacks, profiling, graph capture off or not possible). */
+static int run_interval_on_device(lgb_ctx *c, int analytical, int *rc)
+{
+  long long s0;
+  *rc = 0;
+  if (!c->use_graph || c->profiling || c->reduce || (analytical && !c->d.vfield) || c->wgraph_failed) return 0;
+  if (c->wgraph_valid && c->wgraph_mode != analytical) invalidate_graph(c);
+  if (!c->wgraph_valid) {
+    cudaGraph_t g = NULL, body;
+    cudaGraphConditionalHandle h;
+    struct cudaGraphNodeParams p;
+    cudaGraphNode_t node;
+    long long l0 = lgb_launch_count(), e0 = c->eval_launches;
+    int ok = cudaGraphCreate(&g, 0) == cudaSuccess &&
+             cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault) == cudaSuccess;
+    if (ok) {
+      memset(&p, 0, sizeof(p));
+      p.type = cudaGraphNodeTypeConditional;
+      p.conditional.handle = h;
+      p.conditional.type = cudaGraphCondTypeWhile;
+      p.conditional.size = 1;
+      ok = cudaGraphAddNode(&node, g, NULL, NULL, 0, &p) == cudaSuccess;
+    }
+    if (ok) {
+      body = p.conditional.phGraph_out[0];
+      ok = cudaStreamBeginCaptureToGraph(c->stream, body, NULL, NULL, 0, cudaStreamCaptureModeThreadLocal) ==
+           cudaSuccess;
+      if (ok) {
+        int r = step_sequence(c, analytical);
+        if (!r) r = lgb_op_loop_cond(&c->d, (unsigned long long)h, c->stream);
+        ok = (cudaStreamEndCapture(c->stream, &body) == cudaSuccess) && !r;
+      }
+    }
+    c->wgraph_eval_launches = c->eval_launches - e0;
+    c->eval_launches = e0;
+    c->wgraph_launches = lgb_launch_count() - l0;
+    c->launch_base += c->wgraph_launches; /* captured, not run */
+    if (ok) ok = cudaGraphInstantiate(&c->wgraph, g, 0) == cudaSuccess;
+    if (g) cudaGraphDestroy(g);
+    if (!ok) {
+      cudaGetLastError();
+      c->wgraph_failed = 1; /* keep stepping from the host */
+      return 0;
+    }
+    c->wgraph_valid = 1;
+    c->wgraph_mode = analytical;
+  }
+  s0 = c->hctrl->steps;
+  CU(cudaGraphLaunch(c->wgraph, c->stream));
+  CU(cudaMemcpyAsync(c->hctrl, c->d.ctrl, sizeof(lgb_ctrl), cudaMemcpyDeviceToHost, c->stream));
+  CU(cudaStreamSynchronize(c->stream));
+  c->launches_graph += (c->hctrl->steps - s0) * c->wgraph_launches;
+  c->eval_launches += (c->hctrl->steps - s0) * c->wgraph_eval_launches;
+  if (c->hctrl->factor_error) *rc = check_factor_error(c);
+  else *rc = check_eval_error(c);
+  return 1;
+}
+
 static int advection_loop(lgb_ctx *c, double t, double t_next, int analytical, int keep)
 {
   lgb_dev *d = &c->d;
@@ -1201,6 +1271,8 @@ static int advection_loop(lgb_ctx *c, double t, double t_next, int analytical, i
   c->hctrl->t_next = t_next;
   c->hctrl->scheme = c->scheme;
   c->hctrl->pp_hmin = 1e-10 * (t_next - t);
+  c->hctrl->loop_iter = 0;
+  c->hctrl->loop_cap = 1 << 20;
   CU(cudaMemcpyAsync(d->ctrl, c->hctrl, sizeof(lgb_ctrl), cudaMemcpyHostToDevice, c->stream));
   /* AdvectionInitializeTimestepVelocity, then the CFL of that velocity */
   OP(lgb_op_ctrl(d, LGB_CTRL_RESET_CFL, c->stream));
@@ -1216,6 +1288,13 @@ static int advection_loop(lgb_ctx *c, double t, double t_next, int analytical, i
     CU(cudaMemcpyAsync(c->hctrl, d->ctrl, sizeof(lgb_ctrl), cudaMemcpyDeviceToHost, c->stream));
     CU(cudaStreamSynchronize(c->stream));
     TRY(couple_ranks(c, 0)); /* the first step's CFL step over all ranks */
+  }
+  if (t < t_next) {
+    int rc;
+    if (run_interval_on_device(c, analytical, &rc)) {
+      TRY(rc);
+      t = c->hctrl->t; /* beyond the iteration limit the host continues step by step */
+    }
   }
   while (t < t_next) {
     TRY(run_step(c, analytical));
@@ -1633,6 +1712,7 @@ LAGRBF_EXPORT int lagrbf_gpu_get_stats(void *ctx, lagrbf_stats_t *st)
   st->dt = c->hctrl->dt_adv;
   st->chunk_cap = c->d.chunk_cap;
   st->records = c->d.rec32 != NULL;
+  st->device_loop = c->wgraph_valid;
   if (c->d.cond_on) {
     double sm[3];
     TRY(lagrbf_gpu_get_condition(ctx, NULL, sm));

@@ -104,6 +104,8 @@ typedef struct {
   int eval_error;      /* a bounded wait of the evaluation kernel gave up */
   int pp_left;         /* per-particle Dormand-Prince: particles still short of t_next   */
   double dt_cfl_ext;   /* > 0: the CFL step agreed over ranks (replaces the local one)     */
+  long long loop_iter; /* internal steps of the current device-side step loop             */
+  long long loop_cap;  /* its limit (the loop then stops and the host continues step by step) */
   double pp_hmin;      /* per-particle Dormand-Prince: steps below this are accepted      */
 } lgb_ctrl;
 
@@ -196,6 +198,10 @@ int lgb_op_pp_init(lgb_dev *d, double t, void *stream);
 int lgb_op_pp_begin(lgb_dev *d, void *stream);
 int lgb_op_pp_accept(lgb_dev *d, void *stream);
 int lgb_op_copy_velocity(lgb_dev *d, void *stream);     /* vel <- fields[:, :dim] */
+/* Condition of the device-side step loop (a conditional while node of the step graph, handle =
+   a cudaGraphConditionalHandle): continue while t < t_next, no error flag is set and the
+   iteration limit is not reached. */
+int lgb_op_loop_cond(lgb_dev *d, unsigned long long handle, void *stream);
 int lgb_op_count_alive(lgb_dev *d, void *stream);
 int lgb_op_velocity_field(lgb_dev *d, void *stream);    /* vel <- analytical field at live particles */
 int lgb_device_info(int *nsm, int *smem_optin);

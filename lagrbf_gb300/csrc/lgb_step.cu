@@ -496,6 +496,20 @@ __global__ void k_ctrl(lgb_ctrl *c, int what)
   }
 }
 
+__global__ void k_loop_cond(lgb_ctrl *c, cudaGraphConditionalHandle h)
+{
+  c->loop_iter += 1;
+  const int go = c->t < c->t_next && !c->factor_error && !c->eval_error && c->loop_iter < c->loop_cap;
+  cudaGraphSetConditional(h, go ? 1u : 0u);
+}
+
+extern "C" int lgb_op_loop_cond(lgb_dev *d, unsigned long long handle, void *stream)
+{
+  k_loop_cond<<<1, 1, 0, (cudaStream_t)stream>>>(d->ctrl, (cudaGraphConditionalHandle)handle);
+  lgb_count_launch(1);
+  return (int)cudaGetLastError();
+}
+
 extern "C" int lgb_op_ctrl(lgb_dev *d, int what, void *stream)
 {
   k_ctrl<<<1, 1, 0, (cudaStream_t)stream>>>(d->ctrl, what);
