@@ -154,6 +154,14 @@ LAGRBF_EXPORT double lagrbf_gpu_fp32_peak_tflops(void);
    patches not factored while on) and summary[3] = {max, median, count} of the non-zero ones. */
 LAGRBF_EXPORT int lagrbf_gpu_set_condition_estimates(void *ctx, int on);
 LAGRBF_EXPORT int lagrbf_gpu_get_condition(void *ctx, double *kappa, double *summary);
+/* Several particle sets on one resident dataset, concurrently: ctx (a fresh context with the same
+   options, no data of its own) uses owner's data swarm, patch set-ups, coefficients, factors and
+   record blocks in place, read-only, on its own stream with its own particles.  The owner needs the
+   option setup_all_patches and a completed interpolation (every patch set up and solved), so that
+   nothing ctx does writes the shared state; lagrbf_fill_swarm of the data on ctx is refused and its
+   coefficient reset does nothing.  The owner must outlive ctx and keep its data unchanged while ctx
+   is in use. */
+LAGRBF_EXPORT int lagrbf_gpu_share_dataset(void *ctx, void *owner);
 /* Coupling of sharded runs (one process and GPU per rank, each holding the whole dataset and a pid
    range of the particles): fn(vals, n, user) must replace vals[0..n) by their element-wise maximum
    over the ranks (e.g. an MPI_Allreduce with MPI_MAX) and return 0.  Each internal step of the
@@ -239,6 +247,8 @@ typedef struct {
   double p50_ms, p99_ms, mean_ms, max_ms; /* submission-to-completion latency of completed jobs */
   double particle_steps, elapsed_s, bytes_in_use;
   int32_t datasets_resident;
+  double queue_p50_ms, queue_p99_ms;      /* submission to start (waiting in the queue)          */
+  double service_p50_ms, service_p99_ms;  /* start to completion (set-up if any, steps, output)  */
 } lagrbf_server_stats_t;
 /* Worker threads (one context and CUDA stream per running job) admit queued jobs first in, first
    out as the device-memory budget and their dataset allow; a job may pass a waiting one that does

@@ -97,6 +97,7 @@ def register_functions(clib):
     reg("lagrbf_options_get_value", ctypes.c_int, [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_int32])
     # GPU extension
     reg("lagrbf_gpu_set_profiling", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int])
+    reg("lagrbf_gpu_share_dataset", ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p])
     reg("lagrbf_gpu_set_step_reduce", ctypes.c_int, [ctypes.c_void_p, STEP_REDUCE, ctypes.c_void_p])
     reg("lagrbf_gpu_set_condition_estimates", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int])
     reg("lagrbf_gpu_get_condition", ctypes.c_int, [ctypes.c_void_p, real_pn, real_pn])

@@ -235,6 +235,13 @@ class LagRBFCtx:
     def set_profiling(self, on):
         self._check(self._cf["lagrbf_gpu_set_profiling"](self.ctx, int(bool(on))), "lagrbf_gpu_set_profiling")
 
+    def share_dataset(self, owner):
+        """Use owner's resident dataset in place, read-only (lagrbf_gpu_share_dataset); owner needs
+        setup_all_patches and a completed interpolation, and must outlive this context."""
+        self._check(self._cf["lagrbf_gpu_share_dataset"](self.ctx, owner.ctx), "lagrbf_gpu_share_dataset")
+        self._shared_owner = owner
+        self.data_filled = True
+
     def set_step_reduce(self, fn):
         """Coupling of sharded runs (lagrbf_gpu_set_step_reduce): fn(vals) replaces the numpy array
         vals by its element-wise maximum over the ranks; None removes it."""

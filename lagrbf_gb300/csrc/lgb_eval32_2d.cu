@@ -31,11 +31,17 @@ static int launch32(const EvalParams &P, int grid, cudaStream_t s)
 template <int DIM, int KER>
 static int launch_rec(const EvalParams &P, int grid, cudaStream_t s)
 {
-  static size_t attr = 0;
+  /* the attribute is set once to the device's largest opt-in size (threads racing on it all set the
+     same value; a per-call size could shrink it under another thread's launch) */
+  static int attr = 0;
   const size_t smem = (size_t)EVR_NB * P.budget * sizeof(float) + (size_t)(P.chunk_cap / 2) * ((1 << DIM) + 1) * 8;
-  if (smem > attr) {
-    cudaFuncSetAttribute(k_eval_rec<DIM, DIM, KER>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    attr = smem;
+  if (!attr) {
+    int dev = 0, optin = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    cudaFuncSetAttribute(k_eval_rec<DIM, DIM, KER>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         optin - 8192);
+    attr = 1;
   }
   k_eval_rec<DIM, DIM, KER><<<grid, P.chunk_cap / 2, smem, s>>>(P);
   return (int)cudaGetLastError();

@@ -229,7 +229,7 @@ typedef int (*vfn_t)(double *, double *, void *);
 typedef int (*vfnb_t)(int32_t, int32_t, double *, double *, void *);
 
 #define NPROF 16
-typedef struct {
+typedef struct lgb_ctx_s {
   lgb_dev d;
   cudaStream_t stream;
   /* configuration (LagRBFSetFromOptions) */
@@ -251,6 +251,9 @@ typedef struct {
   vfn_t vfn;
   vfnb_t vfnb;
   void *vuser;
+  /* dataset borrowed from another context (lagrbf_gpu_share_dataset): read-only, not freed here */
+  struct lgb_ctx_s *shared_from;
+  int all_ready;       /* setup_all_patches and every patch set up and solved for the current data */
   /* coupling of sharded runs: element-wise max over the ranks of {-(CFL step), DOPRI error} */
   int (*reduce)(double *, int32_t, void *);
   void *ruser;
@@ -306,6 +309,32 @@ static void free_particles(lgb_dev *d)
   d->np_cap = 0;
 }
 
+/* The dataset arrays a sharing context borrows (lagrbf_gpu_share_dataset). */
+static void borrow_dataset(lgb_dev *d, const lgb_dev *o)
+{
+  d->xd = o->xd; d->fd = o->fd; d->xs = o->xs; d->fs = o->fs; d->xr = o->xr;
+  d->cell_d = o->cell_d; d->cstart = o->cstart; d->sorted = o->sorted;
+  d->pm = o->pm; d->slot = o->slot; d->setup = o->setup; d->solved = o->solved;
+  d->coff = o->coff; d->foff = o->foff; d->c64 = o->c64; d->c32 = o->c32; d->fac = o->fac;
+  d->rec32 = o->rec32; d->rec_off = o->rec_off;
+  d->nd = o->nd; d->max_cell_pts = o->max_cell_pts; d->max_patch = o->max_patch;
+  d->coef_cap = o->coef_cap; d->fac_cap = o->fac_cap; d->rec_cap = o->rec_cap; d->rec_fp = o->rec_fp;
+  d->keep_factors = o->keep_factors;
+}
+
+static void unborrow_dataset(lgb_dev *d)
+{
+  d->xd = d->fd = d->xs = d->fs = NULL;
+  d->xr = NULL;
+  d->cell_d = d->cstart = d->sorted = NULL;
+  d->pm = d->slot = d->setup = d->solved = NULL;
+  d->coff = d->foff = NULL;
+  d->c64 = d->fac = NULL;
+  d->c32 = d->rec32 = NULL;
+  d->rec_off = NULL;
+  d->nd = 0;
+}
+
 static void destroy_ctx(lgb_ctx *c)
 {
   lgb_dev *d = &c->d;
@@ -313,6 +342,7 @@ static void destroy_ctx(lgb_ctx *c)
   if (!c) return;
   if (c->stream) cudaStreamSynchronize(c->stream);
   invalidate_graph(c);
+  if (c->shared_from) unborrow_dataset(d);
   free_data(d);
   free_particles(d);
   DFREE(d->cstart); DFREE(d->dfill); DFREE(d->pm); DFREE(d->slot); DFREE(d->setup); DFREE(d->solved);
@@ -764,6 +794,9 @@ static int fill_data(lgb_ctx *c, int n, const double *coords, const double *valu
   lgb_dev *d = &c->d;
   int dim = d->g.dim, F = d->F, err = 0, same_coords;
   int old = d->nd;
+  if (c->shared_from)
+    return set_error(LAGRBF_ERR_ARG_WRONGSTATE, "the data swarm is shared from another context (read-only)");
+  c->all_ready = 0;
   TRY(check_box(&d->g, n, coords, (c->hx_d && n == d->nd && n > 0) ? c->hx_d : NULL, &same_coords));
   TRY(grow_pids(&c->pid_d, &c->pid_d_cap, old, n));
   if (pidx) memcpy(c->pid_d, pidx, sizeof(int64_t) * (size_t)n);
@@ -1009,12 +1042,16 @@ static int do_interpolation(lgb_ctx *c)
   prof_collect(c, &c->eval_ms);
   CU(cudaMemcpyAsync(c->hctrl, c->d.ctrl, sizeof(lgb_ctrl), cudaMemcpyDeviceToHost, c->stream));
   CU(cudaStreamSynchronize(c->stream));
-  return check_eval_error(c);
+  TRY(check_eval_error(c));
+  if (d->setup_all && !c->shared_from) c->all_ready = 1; /* every patch set up and solved */
+  return 0;
 }
 
 static int reset_coefficients(lgb_ctx *c)
 {
   lgb_dev *d = &c->d;
+  if (c->shared_from) return 0; /* the patch set-ups belong to the dataset's owner */
+  c->all_ready = 0;
   /* LagRBF_PartitionsReset: A_KSP_ASMB destroys the patch set-ups, the others only the solution */
   if (d->solve_method == LGB_A_KSP_ASMB) {
     CU(cudaMemsetAsync(d->setup, 0, sizeof(int) * (size_t)d->g.nnodes, c->stream));
@@ -1589,6 +1626,38 @@ LAGRBF_EXPORT int lagrbf_gpu_set_precision(void *ctx, int fp32)
   if (!c) return set_error(LAGRBF_ERR_ARG_NULL, "context is NULL");
   CU(cudaStreamSynchronize(c->stream));
   c->d.prec = fp32 ? LGB_PREC_FP32 : LGB_PREC_FP64;
+  invalidate_graph(c);
+  return 0;
+}
+
+LAGRBF_EXPORT int lagrbf_gpu_share_dataset(void *ctx, void *owner)
+{
+  lgb_ctx *c = (lgb_ctx *)ctx, *o = (lgb_ctx *)owner;
+  lgb_dev *d;
+  int k;
+  if (!c || !o) return set_error(LAGRBF_ERR_ARG_NULL, "context is NULL");
+  d = &c->d;
+  if (c == o || c->shared_from || o->shared_from)
+    return set_error(LAGRBF_ERR_ARG_WRONGSTATE, "dataset sharing: one owner, one level of sharing");
+  if (!o->data_filled || !o->all_ready)
+    return set_error(LAGRBF_ERR_ARG_WRONGSTATE,
+                     "dataset sharing: the owner needs setup_all_patches and a completed interpolation");
+  if (c->data_filled || d->nd > 0) return set_error(LAGRBF_ERR_ARG_WRONGSTATE, "dataset sharing: ctx has its own data");
+  if (d->g.dim != o->d.g.dim || d->g.kernel != o->d.g.kernel || d->F != o->d.F || d->g.eps_r != o->d.g.eps_r ||
+      d->g.eps_w != o->d.g.eps_w || d->solve_method != o->d.solve_method)
+    return set_error(LAGRBF_ERR_ARG_WRONG, "dataset sharing: different mesh, kernel or fields");
+  for (k = 0; k < 3; k++)
+    if (d->g.n[k] != o->d.g.n[k] || d->g.O[k] != o->d.g.O[k] || d->g.L[k] != o->d.g.L[k])
+      return set_error(LAGRBF_ERR_ARG_WRONG, "dataset sharing: different PU mesh");
+  CU(cudaStreamSynchronize(o->stream));
+  CU(cudaStreamSynchronize(c->stream));
+  free_data(d);
+  DFREE(d->cstart); DFREE(d->pm); DFREE(d->slot); DFREE(d->setup); DFREE(d->solved);
+  DFREE(d->coff); DFREE(d->foff); DFREE(d->c64); DFREE(d->c32); DFREE(d->fac); DFREE(d->rec32); DFREE(d->rec_off);
+  borrow_dataset(d, &o->d);
+  d->setup_all = 1; /* every patch of the borrowed dataset is set up: nothing is queued */
+  c->shared_from = o;
+  c->data_filled = 1;
   invalidate_graph(c);
   return 0;
 }

@@ -7,8 +7,10 @@
  * budget and the job's dataset allow, each job on its own context (its own CUDA stream, its own
  * captured step graph), so jobs that arrive while others run are admitted as memory frees up and
  * their work overlaps on the device.  Datasets with an id stay resident after their job (data,
- * patch set-ups, coefficients, record blocks): a later job on the same id skips the set-up.  Idle
- * resident datasets are evicted, least recently used first, when a job needs their memory.
+ * every patch set up and solved, coefficients, record blocks): a later job on the same id skips
+ * the set-up, and jobs on a dataset whose context is busy run at the same time on contexts that
+ * share it read-only (lagrbf_gpu_share_dataset).  Idle resident datasets are evicted, least
+ * recently used first, when a job needs their memory.
  *
  * The server is a client of the context API of this library (lagrbf_create ... lagrbf_output);
  * a job's result is its particle positions after the last step, by pid.
@@ -26,6 +28,9 @@
 int lgb_set_error_msg(int code, const char *msg);
 int lgb_ctx_set_scheme(void *ctx, int scheme, double dt);
 
+/* Device bytes of a context that shares a resident dataset, beyond its particles. */
+#define SHARE_BYTES (64LL << 20)
+
 typedef struct srv_job {
   int64_t id;
   lagrbf_job_t spec;
@@ -34,15 +39,17 @@ typedef struct srv_job {
   int state;              /* 0 queued, 1 running, 2 done, 3 collected */
   int rc;
   char err[256];
-  double t_submit, t_done;
+  double t_submit, t_start, t_done;
   double pss;             /* particle-steps advanced */
   struct srv_job *next;   /* FIFO */
 } srv_job;
 
 typedef struct {
   int64_t id;             /* > 0 */
-  void *ctx;
-  int busy;
+  void *ctx;              /* the owner context (holds the dataset)                           */
+  int busy;               /* the owner context runs a job                                    */
+  int ready;              /* every patch set up and solved: other jobs may share the dataset */
+  int users;              /* running jobs on the dataset (owner and sharing contexts)        */
   long long bytes;        /* estimate held by this context */
   int np_cap;
   double last_used;
@@ -59,8 +66,8 @@ typedef struct {
   long long budget, in_use;
   int nworkers, stop;
   pthread_t *threads;
-  /* statistics since the last reset */
-  double *lat;
+  /* statistics since the last reset: latency, queue wait and service time of completed jobs */
+  double *lat, *qwait, *svc;
   int64_t nlat, caplat, failed;
   double pss, t0, t_last;
 } srv_t;
@@ -117,6 +124,7 @@ static void drop_ds(srv_t *s, int i)
 static long long job_extra(srv_t *s, const srv_job *j)
 {
   srv_dataset *d = find_ds(s, j->spec.dataset_id);
+  if (d && d->busy) return particle_bytes(&j->spec) + SHARE_BYTES; /* a context sharing the dataset */
   if (d) return (j->spec.np > d->np_cap) ? pbytes(j->spec.np, j->spec.dim) - pbytes(d->np_cap, j->spec.dim) : 0;
   return dataset_bytes(&j->spec) + particle_bytes(&j->spec);
 }
@@ -126,7 +134,7 @@ static long long job_extra(srv_t *s, const srv_job *j)
 static int evictable(srv_t *s, const srv_dataset *d, int64_t keep)
 {
   const srv_job *q;
-  if (d->busy || d->id == keep) return 0;
+  if (d->busy || d->users || d->id == keep) return 0;
   for (q = s->head; q; q = q->next)
     if (q->spec.dataset_id == d->id && !q->xd) return 0;
   return 1;
@@ -160,7 +168,7 @@ static srv_job *pick(srv_t *s)
   double t = now_s();
   for (j = s->head; j; prev = j, j = j->next) {
     srv_dataset *d = find_ds(s, j->spec.dataset_id);
-    int ok = !(d && d->busy);
+    int ok = !(d && d->busy && !d->ready); /* a busy dataset is shared once it is ready */
     if (ok && j->spec.dataset_id > 0 && !d && !j->xd) ok = 0; /* waits for its dataset to be resident */
     if (ok) ok = make_room(s, job_extra(s, j), j->spec.dataset_id);
     if (ok) {
@@ -201,6 +209,8 @@ static void *create_job_ctx(srv_t *s, const lagrbf_job_t *j)
   snprintf(v, sizeof(v), "%.17g", j->dt); lagrbf_options_set_value("dt", v);
   snprintf(v, sizeof(v), "%.17g", j->cfl > 0 ? j->cfl : 0.3); lagrbf_options_set_value("cfl_fac", v);
   lagrbf_options_set_value("solve_method", "2");
+  /* resident datasets set up every patch, so that later jobs can share them read-only */
+  if (j->dataset_id > 0) lagrbf_options_set_value("setup_all_patches", "true");
   lagrbf_options_set_value("eval_precision", j->fp32 ? "fp32" : "fp64");
   ctx = lagrbf_create();
   if (!ctx) snprintf(v, sizeof(v), "%s", lagrbf_gpu_last_error());
@@ -210,8 +220,21 @@ static void *create_job_ctx(srv_t *s, const lagrbf_job_t *j)
   return ctx;
 }
 
-/* Runs one job on ctx (the dataset is filled when `fill` is set). */
-static int run_job(void *ctx, srv_job *j, int fill)
+static void mark_ready(srv_t *s, int64_t id)
+{
+  srv_dataset *d;
+  pthread_mutex_lock(&s->lock);
+  d = find_ds(s, id);
+  if (d && d->ctx && !d->ready) {
+    d->ready = 1;
+    pthread_cond_broadcast(&s->cv_work);
+  }
+  pthread_mutex_unlock(&s->lock);
+}
+
+/* Runs one job on ctx (the dataset is filled when `fill` is set; an owner context of a resident
+   dataset marks it ready for sharing once its interpolation has set up every patch). */
+static int run_job(srv_t *s, void *ctx, srv_job *j, int fill, int owner)
 {
   const lagrbf_job_t *p = &j->spec;
   lagrbf_stats_t st0, st1;
@@ -228,6 +251,7 @@ static int run_job(void *ctx, srv_job *j, int fill)
   free(pid);
   if (rc) return rc;
   if ((rc = lagrbf_interpolation(ctx))) return rc;
+  if (owner && p->dataset_id > 0) mark_ready(s, p->dataset_id);
   if ((rc = lagrbf_gpu_get_stats(ctx, &st0))) return rc;
   for (k = 0; k < p->nsteps && !rc; k++, t += p->dt) rc = lagrbf_gpu_advect_resident(ctx, t, t + p->dt);
   if (rc) return rc;
@@ -243,21 +267,28 @@ static void *worker(void *arg)
   for (;;) {
     srv_job *j = NULL;
     srv_dataset *d;
-    void *ctx = NULL;
-    int fill = 0, cached, rc;
+    void *ctx = NULL, *share = NULL;
+    int fill = 0, cached, rc, owner = 0;
     long long extra;
     while (!s->stop && !(j = pick(s))) pthread_cond_wait(&s->cv_work, &s->lock);
     if (!j) break;
     j->state = 1;
+    j->t_start = now_s();
     extra = job_extra(s, j);
     s->in_use += extra;
     d = find_ds(s, j->spec.dataset_id);
     cached = j->spec.dataset_id > 0;
-    if (d) {
+    if (d && d->busy) {
+      /* the owner context is running: share its dataset from a context of this job */
+      d->users++;
+      share = d->ctx;
+    } else if (d) {
       d->busy = 1;
+      d->users++;
       d->bytes += extra;
       if (j->spec.np > d->np_cap) d->np_cap = j->spec.np;
       ctx = d->ctx;
+      owner = 1;
     } else if (cached) {
       if (s->nds == s->capds) {
         int cap = s->capds ? 2 * s->capds : 16;
@@ -271,28 +302,47 @@ static void *worker(void *arg)
       memset(d, 0, sizeof(*d));
       d->id = j->spec.dataset_id;
       d->busy = 1;
+      d->users = 1;
       d->bytes = extra;
       d->np_cap = j->spec.np;
+      owner = 1;
     }
     pthread_mutex_unlock(&s->lock);
 
-    if (!ctx) {
+    rc = 0;
+    if (share) {
+      ctx = create_job_ctx(s, &j->spec);
+      rc = ctx ? lagrbf_gpu_share_dataset(ctx, share) : LAGRBF_ERR_GPU;
+    } else if (!ctx) {
       ctx = create_job_ctx(s, &j->spec);
       fill = 1;
+      if (!ctx) rc = LAGRBF_ERR_GPU;
+      if (ctx && owner) { /* the dataset's owner context, known before it is marked ready */
+        pthread_mutex_lock(&s->lock);
+        d = find_ds(s, j->spec.dataset_id);
+        if (d && !d->ctx) d->ctx = ctx;
+        pthread_mutex_unlock(&s->lock);
+      }
     }
-    rc = ctx ? run_job(ctx, j, fill) : LAGRBF_ERR_GPU;
+    if (!rc) rc = run_job(s, ctx, j, fill, owner);
     if (rc) snprintf(j->err, sizeof(j->err), "%s", lagrbf_gpu_last_error());
 
     pthread_mutex_lock(&s->lock);
     d = find_ds(s, j->spec.dataset_id);
-    if (d && d->busy && (!d->ctx || d->ctx == ctx)) {
+    if (d && owner && d->busy && (!d->ctx || d->ctx == ctx)) {
       d->ctx = ctx;
       d->busy = 0;
+      d->users--;
       d->last_used = now_s();
-      if (rc) drop_ds(s, (int)(d - s->ds)); /* a failed context is not reused */
+      if (rc && d->users == 0) drop_ds(s, (int)(d - s->ds)); /* a failed context is not reused */
+      else if (rc) d->ready = 0;
     } else {
       if (ctx) lagrbf_destroy(ctx);
       s->in_use -= extra;
+      if (d && share) {
+        d->users--;
+        d->last_used = now_s();
+      }
     }
     j->rc = rc;
     j->t_done = now_s();
@@ -304,9 +354,19 @@ static void *worker(void *arg)
       if (s->nlat == s->caplat) {
         int64_t cap = s->caplat ? 2 * s->caplat : 1024;
         double *nl = (double *)realloc(s->lat, sizeof(double) * (size_t)cap);
-        if (nl) { s->lat = nl; s->caplat = cap; }
+        double *nq = (double *)realloc(s->qwait, sizeof(double) * (size_t)cap);
+        double *ns = (double *)realloc(s->svc, sizeof(double) * (size_t)cap);
+        if (nl) s->lat = nl;
+        if (nq) s->qwait = nq;
+        if (ns) s->svc = ns;
+        if (nl && nq && ns) s->caplat = cap;
       }
-      if (s->nlat < s->caplat) s->lat[s->nlat++] = 1e3 * (j->t_done - j->t_submit);
+      if (s->nlat < s->caplat) {
+        s->lat[s->nlat] = 1e3 * (j->t_done - j->t_submit);
+        s->qwait[s->nlat] = 1e3 * (j->t_start - j->t_submit);
+        s->svc[s->nlat] = 1e3 * (j->t_done - j->t_start);
+        s->nlat++;
+      }
       s->pss += j->pss;
       s->t_last = j->t_done;
     }
@@ -464,6 +524,14 @@ LAGRBF_EXPORT int lagrbf_server_stats(void *srv, lagrbf_server_stats_t *st)
       st->p99_ms = c[(int64_t)ceil(0.99 * (double)s->nlat) - 1];
       st->mean_ms = sum / (double)s->nlat;
       st->max_ms = c[s->nlat - 1];
+      memcpy(c, s->qwait, sizeof(double) * (size_t)s->nlat);
+      qsort(c, (size_t)s->nlat, sizeof(double), cmp_d);
+      st->queue_p50_ms = c[(int64_t)ceil(0.50 * (double)s->nlat) - 1];
+      st->queue_p99_ms = c[(int64_t)ceil(0.99 * (double)s->nlat) - 1];
+      memcpy(c, s->svc, sizeof(double) * (size_t)s->nlat);
+      qsort(c, (size_t)s->nlat, sizeof(double), cmp_d);
+      st->service_p50_ms = c[(int64_t)ceil(0.50 * (double)s->nlat) - 1];
+      st->service_p99_ms = c[(int64_t)ceil(0.99 * (double)s->nlat) - 1];
       free(c);
     }
   }
@@ -512,7 +580,7 @@ LAGRBF_EXPORT void lagrbf_server_destroy(void *srv)
     srv_job *j = s->jobs[k];
     free(j->xd); free(j->fd); free(j->xp); free(j->result); free(j);
   }
-  free(s->jobs); free(s->ds); free(s->lat); free(s->threads);
+  free(s->jobs); free(s->ds); free(s->lat); free(s->qwait); free(s->svc); free(s->threads);
   pthread_mutex_destroy(&s->lock);
   pthread_mutex_destroy(&s->create_lock);
   pthread_cond_destroy(&s->cv_work);

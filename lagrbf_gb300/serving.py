@@ -25,7 +25,8 @@ class ServerStats(ctypes.Structure):
         ("queued", ctypes.c_int64), ("running", ctypes.c_int64), ("p50_ms", ctypes.c_double),
         ("p99_ms", ctypes.c_double), ("mean_ms", ctypes.c_double), ("max_ms", ctypes.c_double),
         ("particle_steps", ctypes.c_double), ("elapsed_s", ctypes.c_double), ("bytes_in_use", ctypes.c_double),
-        ("datasets_resident", ctypes.c_int32),
+        ("datasets_resident", ctypes.c_int32), ("queue_p50_ms", ctypes.c_double), ("queue_p99_ms", ctypes.c_double),
+        ("service_p50_ms", ctypes.c_double), ("service_p99_ms", ctypes.c_double),
     ]
 
     def as_dict(self):

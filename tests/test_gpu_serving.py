@@ -56,3 +56,36 @@ def test_jobs_in_the_mix_match_jobs_alone():
     for a, b in zip(mixed, alone):
         assert np.array_equal(a, b)
         assert np.isfinite(a).all() and (np.abs(a).sum(axis=1) > 0).mean() > 0.9
+
+
+def test_shared_dataset_gives_the_owners_values():
+    """lagrbf_gpu_share_dataset: a context borrowing a resident dataset read-only evaluates a
+    particle set exactly as the owner does; sharing needs a ready owner, and the borrowed data
+    cannot be refilled."""
+    import lagrbf_gb300 as L
+    xd, fd, npu = _datasets()[1]
+    opts = dict(dim=3, npartitions=[npu] * 3, overlap=W.pu_overlap(npu), shape_factor=1.0, kernel=2, nfields=3,
+                eval_precision="fp32", petsc_options={"setup_all_patches": True})
+    xp = W.uniform_points(2000, 3, np.random.default_rng(3))
+    owner = L.LagRBFCtx(**opts)
+    other = L.LagRBFCtx(**opts)
+    with pytest.raises(RuntimeError, match="error code 73"):
+        other.share_dataset(owner)  # the owner has no data yet
+    pid = np.arange(1, len(xp) + 1, dtype=np.int64)
+    owner.fill_data(xd, fd)
+    owner.fill_points(xp[:10], pidx=pid[:10])
+    owner.interpolate_c()
+    other.share_dataset(owner)
+    with pytest.raises(RuntimeError, match="error code 73"):
+        other.fill_data(xd, fd)
+    owner.fill_points(xp, pidx=pid)
+    owner.interpolate_c()
+    other.fill_points(xp, pidx=pid)
+    other.interpolate_c()
+    a = np.zeros((len(xp), 3)); b = np.zeros((len(xp), 3))
+    owner.output(fvals=a)
+    other.output(fvals=b)
+    assert np.array_equal(a, b) and np.abs(a).max() > 0
+    del other
+    owner.fill_points(xp[:5], pidx=pid[:5])
+    owner.interpolate_c()  # the owner is unaffected by the sharing context's teardown
