@@ -390,13 +390,17 @@ __global__ void k_mark(lgb_geom g, int np, const int *__restrict__ cell, const i
   }
 }
 
-__global__ void k_compact(int nnodes, int *__restrict__ need, int *__restrict__ work, int *__restrict__ nwork)
+/* Queued patches into the work-list region of their size class (cls_off); nwork counts them all. */
+__global__ void k_compact(int nnodes, int *__restrict__ need, const int *__restrict__ pm,
+                          const int *__restrict__ cls_off, int *__restrict__ work, lgb_ctrl *ctrl)
 {
   int node = blockIdx.x * blockDim.x + threadIdx.x;
   if (node >= nnodes) return;
   if (need[node]) {
     need[node] = 0;
-    work[atomicAdd(nwork, 1)] = node;
+    const int c = lgb_patch_class(pm[node]);
+    work[cls_off[c] + atomicAdd(&ctrl->nwork_c[c], 1)] = node;
+    atomicAdd(&ctrl->nwork, 1);
   }
 }
 
@@ -412,6 +416,7 @@ extern "C" int lgb_op_mark_patches(lgb_dev *d, void *stream)
 {
   cudaStream_t s = (cudaStream_t)stream;
   cudaMemsetAsync(&d->ctrl->nwork, 0, sizeof(int), s);
+  cudaMemsetAsync(d->ctrl->nwork_c, 0, sizeof(int) * LGB_NCLS, s);
   if (d->setup_all) {
     k_mark_all<<<lgb_cdiv(d->g.nnodes, 256), 256, 0, s>>>(d->g.nnodes, d->setup, d->solved, d->need);
     lgb_count_launch(1);
@@ -419,7 +424,8 @@ extern "C" int lgb_op_mark_patches(lgb_dev *d, void *stream)
     k_mark<<<lgb_cdiv(d->np, 256), 256, 0, s>>>(d->g, d->np, d->cell_p, d->alive, d->setup, d->solved, d->need);
     lgb_count_launch(1);
   }
-  k_compact<<<lgb_cdiv(d->g.nnodes, 256), 256, 0, s>>>(d->g.nnodes, d->need, d->work, &d->ctrl->nwork);
+  k_compact<<<lgb_cdiv(d->g.nnodes, 256), 256, 0, s>>>(d->g.nnodes, d->need, d->pm, d->cls_off_dev, d->work,
+                                                        d->ctrl);
   lgb_count_launch(1);
   LGB_CHECK_LAUNCH();
   return 0;

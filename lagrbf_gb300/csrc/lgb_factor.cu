@@ -6,8 +6,11 @@
  * MatCholeskyFactor / KSP preonly+PCCHOLESKY (partition_factor.c:37-55, partition_ksp.c:115-172) and
  * the RHS gather + MatMatSolve (partition_factor.c:57-135).
  *
- * One CTA per queued patch at a time (persistent grid over the work list, (1024 / LGB_FACT_T)
- * CTAs per SM, so the launch is graph-capturable with a device-side count).  The patch matrix is
+ * Patches are queued by size class (LGB_NCLS classes of sizes up to 32, 64, ..., 2048 and beyond);
+ * each class is one launch of a persistent grid over its work list (graph-capturable with a
+ * device-side count), with the class's CTA size from the measured table (lgb_factor_tune.h), its
+ * own workspace slot size (the class's largest patch) and as many CTAs as fit 1024 threads per SM
+ * within the workspace budget.  The patch matrix is
  * assembled column-major into a per-CTA workspace slot (lower triangle), factored in panels of
  * CHOL_NB columns (left-looking inside a panel, then a tiled update of the trailing triangle), then
  * the F right-hand sides are solved together.  FP64 throughout: the collocation systems are
@@ -23,7 +26,6 @@
  */
 #include "lgb_common.cuh"
 
-#define FACT_T LGB_FACT_T
 #define CHOL_NB 16 /* columns per Cholesky panel */
 
 struct FactorParams {
@@ -31,7 +33,8 @@ struct FactorParams {
   int F, keep;
   const int *cstart;
   const double *xs, *fs;
-  const int *pm, *slot, *work;
+  const int *pm, *slot, *work;  /* work: the nodes of one patch-size class, *nwork of them */
+  const int *nwork;
   const long long *coff, *foff;
   int *setup, *solved;
   double *c64, *fac, *ws;
@@ -197,7 +200,7 @@ __device__ void chol_solve(const double *L, int m, int F, double *B, double *D, 
   }
 }
 
-/* ---- block reductions (FACT_T threads; red: 32 doubles of shared memory) ---- */
+/* ---- block reductions (blockDim.x threads; red: 32 doubles of shared memory) ---- */
 __device__ double blk_reduce(double v, double *red, bool is_max)
 {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
@@ -244,15 +247,15 @@ __device__ double inv_norm1_estimate(const double *L, int m, double *v, double *
                                      int *ired)
 {
   const int tid = threadIdx.x;
-  for (int i = tid; i < m; i += FACT_T) v[i] = 1.0 / m;
+  for (int i = tid; i < m; i += blockDim.x) v[i] = 1.0 / m;
   __syncthreads();
   chol_solve_group<false, 1>(L, m, v, D, Y);
   double s = 0.0;
-  for (int i = tid; i < m; i += FACT_T) s += fabs(v[i]);
+  for (int i = tid; i < m; i += blockDim.x) s += fabs(v[i]);
   double est = blk_reduce(s, red, false);
   int jprev = -1;
   for (int it = 0; it < 5; it++) {
-    for (int i = tid; i < m; i += FACT_T) u[i] = (v[i] >= 0.0) ? 1.0 : -1.0;
+    for (int i = tid; i < m; i += blockDim.x) u[i] = (v[i] >= 0.0) ? 1.0 : -1.0;
     __syncthreads();
     chol_solve_group<false, 1>(L, m, u, D, Y);
     int j;
@@ -260,32 +263,34 @@ __device__ double inv_norm1_estimate(const double *L, int m, double *v, double *
     double ztx;
     if (jprev < 0) {
       double t = 0.0;
-      for (int i = tid; i < m; i += FACT_T) t += u[i];
+      for (int i = tid; i < m; i += blockDim.x) t += u[i];
       ztx = blk_reduce(t, red, false) / m;
     } else {
       ztx = u[jprev];
     }
     if (it > 0 && zmax <= ztx) break;
-    for (int i = tid; i < m; i += FACT_T) v[i] = (i == j) ? 1.0 : 0.0;
+    for (int i = tid; i < m; i += blockDim.x) v[i] = (i == j) ? 1.0 : 0.0;
     __syncthreads();
     chol_solve_group<false, 1>(L, m, v, D, Y);
     s = 0.0;
-    for (int i = tid; i < m; i += FACT_T) s += fabs(v[i]);
+    for (int i = tid; i < m; i += blockDim.x) s += fabs(v[i]);
     const double e2 = blk_reduce(s, red, false);
     if (e2 <= est) break;
     est = e2;
     jprev = j;
   }
-  for (int i = tid; i < m; i += FACT_T) v[i] = ((i & 1) ? -1.0 : 1.0) * (1.0 + (m > 1 ? (double)i / (m - 1) : 0.0));
+  for (int i = tid; i < m; i += blockDim.x) v[i] = ((i & 1) ? -1.0 : 1.0) * (1.0 + (m > 1 ? (double)i / (m - 1) : 0.0));
   __syncthreads();
   chol_solve_group<false, 1>(L, m, v, D, Y);
   s = 0.0;
-  for (int i = tid; i < m; i += FACT_T) s += fabs(v[i]);
+  for (int i = tid; i < m; i += blockDim.x) s += fabs(v[i]);
   const double alt = 2.0 * blk_reduce(s, red, false) / (3.0 * m);
   return fmax(est, alt);
 }
 
-__global__ void __launch_bounds__(FACT_T) k_factor(FactorParams P)
+/* One template per CTA size NT (the patch-size class's entry of the tuning table). */
+template <int NT>
+__global__ void __launch_bounds__(NT) k_factor(FactorParams P)
 {
   __shared__ int s_cstart[8], s_cnt[8], s_off[8];
   __shared__ int s_fail;
@@ -294,7 +299,7 @@ __global__ void __launch_bounds__(FACT_T) k_factor(FactorParams P)
   __shared__ double s_red[32];
   __shared__ int s_ired[32];
   const lgb_geom &g = P.g;
-  const int nwork = P.ctrl->nwork;
+  const int nwork = *P.nwork;
   const int tid = threadIdx.x;
   double *A = P.ws + (size_t)blockIdx.x * P.ws_stride;
   for (int w = blockIdx.x; w < nwork; w += gridDim.x) {
@@ -320,7 +325,7 @@ __global__ void __launch_bounds__(FACT_T) k_factor(FactorParams P)
     double *X = A + (size_t)m * m;     /* m*dim patch coordinates */
     double *B = X + (size_t)m * g.dim; /* m*F right-hand sides / solutions */
     /* gather the patch points (reference patch order) and their values */
-    for (int q = tid; q < m; q += FACT_T) {
+    for (int q = tid; q < m; q += NT) {
       int s = 0;
       while (s < 7 && q >= s_off[s] + s_cnt[s]) s++;
       int src = s_cstart[s] + (q - s_off[s]);
@@ -335,7 +340,7 @@ __global__ void __launch_bounds__(FACT_T) k_factor(FactorParams P)
       for (int j = 0; j < m; j++) {
         const double xj0 = X[(size_t)j * g.dim], xj1 = X[(size_t)j * g.dim + 1];
         const double xj2 = (g.dim == 3) ? X[(size_t)j * g.dim + 2] : 0.0;
-        for (int i = j + tid; i < m; i += FACT_T) {
+        for (int i = j + tid; i < m; i += NT) {
           double dx = X[(size_t)i * g.dim] - xj0, dy = X[(size_t)i * g.dim + 1] - xj1, d2;
           if (g.dim == 3) {
             double dz = X[(size_t)i * g.dim + 2] - xj2;
@@ -349,7 +354,7 @@ __global__ void __launch_bounds__(FACT_T) k_factor(FactorParams P)
       double anorm = 0.0;
       if (P.kappa) {
         double cm = 0.0;
-        for (int j = tid; j < m; j += FACT_T) {
+        for (int j = tid; j < m; j += NT) {
           double cs = 0.0;
           for (int i = j; i < m; i++) cs += fabs(A[(size_t)j * m + i]);
           for (int k = 0; k < j; k++) cs += fabs(A[(size_t)k * m + j]);
@@ -368,7 +373,7 @@ __global__ void __launch_bounds__(FACT_T) k_factor(FactorParams P)
         const int nb = min(CHOL_NB, m - p0), p1 = p0 + nb;
         for (int j = p0; j < p1; j++) {
           const double *Lj = A + j; /* row j: Lj[k*m] = L(j,k) */
-          for (int i = j + tid; i < m; i += FACT_T) {
+          for (int i = j + tid; i < m; i += NT) {
             double s = A[(size_t)j * m + i];
             for (int k = p0; k < j; k++) s -= A[(size_t)k * m + i] * Lj[(size_t)k * m];
             A[(size_t)j * m + i] = s;
@@ -390,20 +395,20 @@ __global__ void __launch_bounds__(FACT_T) k_factor(FactorParams P)
           __syncthreads();
           if (s_fail) break;
           const double rd = s_rd;
-          for (int i = j + 1 + tid; i < m; i += FACT_T) A[(size_t)j * m + i] *= rd;
+          for (int i = j + 1 + tid; i < m; i += NT) A[(size_t)j * m + i] *= rd;
           __syncthreads();
         }
         __syncthreads();
         if (s_fail || p1 >= m) break;
         /* stage the panel's rows (row-major, padded) for the trailing update */
-        for (int t = tid; t < (m - p0) * nb; t += FACT_T) {
+        for (int t = tid; t < (m - p0) * nb; t += NT) {
           const int kk = t / (m - p0), r = t - kk * (m - p0);
           Ps[(size_t)r * (CHOL_NB + 1) + kk] = A[(size_t)(p0 + kk) * m + p0 + r];
         }
         __syncthreads();
         const int T = (m - p1 + 31) / 32, ntile = T * (T + 1) / 2;
         const int lane = tid & 31, warp = tid >> 5;
-        for (int t = warp; t < ntile; t += FACT_T / 32) {
+        for (int t = warp; t < ntile; t += NT / 32) {
           int c = 0, rem = t;
           while (rem >= T - c) { rem -= T - c; c++; }
           const int i = p1 + 32 * (c + rem) + lane, jb = p1 + 32 * c;
@@ -434,7 +439,7 @@ __global__ void __launch_bounds__(FACT_T) k_factor(FactorParams P)
         double *Fk = P.fac + P.foff[node];
         for (int j = 0; j < m; j++) {
           long long base = (long long)j * m - ((long long)j * (j - 1)) / 2; /* packed column j */
-          for (int i = j + tid; i < m; i += FACT_T) Fk[base + (i - j)] = A[(size_t)j * m + i];
+          for (int i = j + tid; i < m; i += NT) Fk[base + (i - j)] = A[(size_t)j * m + i];
         }
       }
       if (tid == 0) {
@@ -450,7 +455,7 @@ __global__ void __launch_bounds__(FACT_T) k_factor(FactorParams P)
       else chol_solve<false>(A, m, F, B, s_diag, s_y);
       /* coefficients [point][field] in both precisions */
       const long long c0 = P.coff[node];
-      for (int q = tid; q < m; q += FACT_T)
+      for (int q = tid; q < m; q += NT)
         for (int f = 0; f < F; f++) {
           double v = B[(size_t)f * m + q];
           P.c64[(size_t)(c0 + q) * F + f] = v;
@@ -468,7 +473,7 @@ __global__ void __launch_bounds__(FACT_T) k_factor(FactorParams P)
 
 extern "C" int lgb_op_factor(lgb_dev *d, void *stream)
 {
-  if (d->nws <= 0) return 0;
+  if (d->nws <= 0 || !d->ws) return 0;
   FactorParams P;
   P.g = d->g;
   P.F = d->F;
@@ -490,7 +495,22 @@ extern "C" int lgb_op_factor(lgb_dev *d, void *stream)
   P.ws_stride = d->ws_stride;
   P.ctrl = d->ctrl;
   P.kappa = d->cond_on ? d->kappa : NULL;
-  k_factor<<<d->nws, FACT_T, 0, (cudaStream_t)stream>>>(P);
-  lgb_count_launch(1);
-  return (int)cudaGetLastError();
+  /* one launch per patch-size class holding patches: its CTA size, grid and workspace slots */
+  for (int c = 0; c < LGB_NCLS; c++) {
+    if (d->cls_cap[c] <= 0 || d->cls_grid[c] <= 0) continue;
+    P.work = d->work + d->cls_off[c];
+    P.nwork = &d->ctrl->nwork_c[c];
+    P.ws_stride = d->cls_stride[c];
+    cudaStream_t s = (cudaStream_t)stream;
+    switch (d->cls_threads[c]) {
+    case 32: k_factor<32><<<d->cls_grid[c], 32, 0, s>>>(P); break;
+    case 64: k_factor<64><<<d->cls_grid[c], 64, 0, s>>>(P); break;
+    case 256: k_factor<256><<<d->cls_grid[c], 256, 0, s>>>(P); break;
+    default: k_factor<128><<<d->cls_grid[c], 128, 0, s>>>(P); break;
+    }
+    lgb_count_launch(1);
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return (int)e;
+  }
+  return 0;
 }

@@ -20,6 +20,7 @@
  * every patch is set up again (the reference would reuse factors built for the old points).
  */
 #include "lgb_internal.h"
+#include "lgb_factor_tune.h"
 #include "../../include/lagrbf.h"
 
 #include <cuda_runtime_api.h>
@@ -349,7 +350,7 @@ static void destroy_ctx(lgb_ctx *c)
   DFREE(d->need); DFREE(d->work); DFREE(d->status); DFREE(d->coff); DFREE(d->foff); DFREE(d->c64); DFREE(d->kappa);
   DFREE(d->c32); DFREE(d->fac); DFREE(d->ws); DFREE(d->pcount); DFREE(d->pstart); DFREE(d->pfill);
   DFREE(d->chunk_start); DFREE(d->scan_tmp); DFREE(d->scan_tmp64); DFREE(d->ctrl);
-  DFREE(d->rec32); DFREE(d->rec_off); DFREE(d->bkey_buf);
+  DFREE(d->rec32); DFREE(d->rec_off); DFREE(d->bkey_buf); DFREE(d->cls_off_dev);
   for (i = 0; i < 2 * NPROF; i++) if (c->ev[i]) cudaEventDestroy(c->ev[i]);
   if (c->hctrl) cudaFreeHost(c->hctrl);
   if (c->stream) cudaStreamDestroy(c->stream);
@@ -508,6 +509,10 @@ static int read_options(lgb_ctx *c)
   opt_bool("dopri_per_particle", &d->dopri_pp);
   d->setup_all = 0;
   opt_bool("setup_all_patches", &d->setup_all);
+  d->factor_threads = 0;
+  if (opt_int("factor_threads", &d->factor_threads) &&
+      !(d->factor_threads == 32 || d->factor_threads == 64 || d->factor_threads == 128 || d->factor_threads == 256))
+    return set_error(LAGRBF_ERR_ARG_OUTOFRANGE, "factor_threads must be 32, 64, 128 or 256");
   d->prec = LGB_PREC_FP64;
   if (opt_str("eval_precision", buf, sizeof(buf))) {
     if (strcmp(buf, "fp32") == 0) d->prec = LGB_PREC_FP32;
@@ -683,6 +688,55 @@ static int grow_pids(int64_t **a, int *cap, int old_n, int n)
   return 0;
 }
 
+/* Patch-size classes of the set-up / solve launches: per class the work-list region (by the number
+   of its patches), the CTA size (option factor_threads, else the measured table), the workspace
+   slot of its largest patch (m^2 + m (dim + F) + 17 m + 32 doubles: matrix, coordinates,
+   right-hand sides, Cholesky panel rows) and a grid of 1024 / T CTAs per SM; the pool holds the
+   largest class grid x slot, at most LGB_FACT_WS_BYTES (a class with bigger slots runs fewer CTAs). */
+#define LGB_FACT_WS_BYTES (4LL << 30)
+static int plan_classes(lgb_ctx *c)
+{
+  lgb_dev *d = &c->d;
+  int nn = d->g.nnodes, i, k, err = 0, cls_m[LGB_NCLS];
+  int *pm = (int *)malloc(sizeof(int) * (size_t)nn);
+  long long pool = 0;
+  if (!pm) return set_error(LAGRBF_ERR_MEM, "out of host memory");
+  CUF(cudaMemcpy(pm, d->pm, sizeof(int) * (size_t)nn, cudaMemcpyDeviceToHost), free(pm));
+  for (k = 0; k < LGB_NCLS; k++) { d->cls_cap[k] = 0; cls_m[k] = 0; }
+  for (i = 0; i < nn; i++) {
+    k = lgb_patch_class(pm[i]);
+    d->cls_cap[k]++;
+    if (pm[i] > cls_m[k]) cls_m[k] = pm[i];
+  }
+  free(pm);
+  d->cls_off[0] = 0;
+  d->nws = 0;
+  for (k = 0; k < LGB_NCLS; k++) {
+    const long long m = cls_m[k] > 0 ? cls_m[k] : 1;
+    const int T = d->factor_threads ? d->factor_threads : lgb_factor_threads[k];
+    long long grid = (long long)(1024 / T) * d->nsm;
+    d->cls_off[k + 1] = d->cls_off[k] + d->cls_cap[k];
+    d->cls_threads[k] = T;
+    d->cls_stride[k] = m * m + m * (d->g.dim + d->F) + m * 17 + 32;
+    if (grid > d->cls_cap[k]) grid = d->cls_cap[k];
+    if (grid * d->cls_stride[k] * 8 > LGB_FACT_WS_BYTES) grid = LGB_FACT_WS_BYTES / (d->cls_stride[k] * 8);
+    if (grid < 1 && d->cls_cap[k] > 0) grid = 1;
+    d->cls_grid[k] = (int)grid;
+    if (grid * d->cls_stride[k] > pool) pool = grid * d->cls_stride[k];
+    if (grid > d->nws) d->nws = (int)grid;
+  }
+  if (!d->cls_off_dev) d->cls_off_dev = (int *)dalloc(sizeof(int) * (LGB_NCLS + 1), &err);
+  if (err) return set_error(LAGRBF_ERR_MEM, "class table allocation failed");
+  CU(cudaMemcpy(d->cls_off_dev, d->cls_off, sizeof(int) * (LGB_NCLS + 1), cudaMemcpyHostToDevice));
+  if (pool > d->ws_stride) {
+    DFREE(d->ws);
+    d->ws = (double *)dalloc(sizeof(double) * (size_t)(pool > 0 ? pool : 1), &err);
+    d->ws_stride = err ? 0 : pool;
+    if (err) { d->nws = 0; return set_error(LAGRBF_ERR_MEM, "factorisation workspace allocation failed"); }
+  }
+  return 0;
+}
+
 static int ensure_pools(lgb_ctx *c)
 {
   lgb_dev *d = &c->d;
@@ -714,22 +768,7 @@ static int ensure_pools(lgb_ctx *c)
       if (err) { d->fac_cap = 0; return set_error(LAGRBF_ERR_MEM, "factor pool allocation failed (%lld doubles)", ftotal); }
     }
   }
-  /* factorisation workspace: per slot m^2 + m*(dim+F) doubles, up to 4 slots per SM within ~4 GB */
-  {
-    long long m = d->max_patch > 0 ? d->max_patch : 1;
-    long long stride = m * m + m * (d->g.dim + d->F) + m * 17 + 32; /* + Cholesky panel rows */
-    long long budget = 4LL << 30;
-    int nws = (1024 / LGB_FACT_T) * d->nsm; /* patches in flight per SM: barriers and loads are hidden by the others */
-    if ((long long)nws * stride * 8 > budget) nws = (int)(budget / (stride * 8));
-    if (nws < 1) nws = 1;
-    if (stride != d->ws_stride || nws != d->nws) {
-      DFREE(d->ws);
-      d->ws_stride = stride;
-      d->nws = nws;
-      d->ws = (double *)dalloc(sizeof(double) * (size_t)(stride * nws), &err);
-      if (err) { d->nws = 0; return set_error(LAGRBF_ERR_MEM, "factorisation workspace allocation failed"); }
-    }
-  }
+  TRY(plan_classes(c));
   return 0;
 }
 

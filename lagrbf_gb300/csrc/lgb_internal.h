@@ -44,8 +44,22 @@ enum { LGB_VF_NONE = 0, LGB_VF_ROTATION = 1, LGB_VF_CELLULAR = 2, LGB_VF_ABC = 3
    and 2 floats per (field, involved patch), padded to 16 bytes. */
 #define LGB_NVSEG(dim) ((dim) == 3 ? 28 : 9)
 #define LGB_REC2_LEN(dim, ninv, fp) (((2 * (dim) + 2 * (ninv) * (fp) + 3) / 4) * 4)
-/* Threads of a patch set-up / solve CTA; (1024 / LGB_FACT_T) CTAs are kept in flight per SM. */
+/* Patch-size classes of the set-up / solve launches: class c holds the patches of up to
+   32 * 2^c points (the last class every larger one); LGB_FACT_T is the CTA size of a class without a
+   measured entry.  A class with CTAs of T threads keeps 1024 / T of them in flight per SM. */
+#define LGB_NCLS 8
 #define LGB_FACT_T 128
+#ifdef __CUDACC__
+#define LGB_HD __host__ __device__
+#else
+#define LGB_HD
+#endif
+static inline LGB_HD int lgb_patch_class(int m)
+{
+  int c = 0;
+  while (c < LGB_NCLS - 1 && m > (32 << c)) c++;
+  return c;
+}
 /* FP32 record of one data point as the gather kernel stages it in shared memory: a header {x, x, y,
    y, z, z, 0, 0} (coordinates relative to the evaluating cell's origin, each twice so that one
    64-bit pair holds a coordinate for two particles), then the coefficients of the ninv corner
@@ -101,6 +115,7 @@ typedef struct {
   int factor_node;     /* patch with that pivot                                    */
   int nfactored;
   double factor_flops;
+  int nwork_c[LGB_NCLS];  /* queued patches of each size class (the class work lists)      */
   int eval_error;      /* a bounded wait of the evaluation kernel gave up */
   int pp_left;         /* per-particle Dormand-Prince: particles still short of t_next   */
   double dt_cfl_ext;   /* > 0: the CFL step agreed over ranks (replaces the local one)     */
@@ -129,7 +144,7 @@ typedef struct {
   double *c64, *fac;
   float *c32;
   int max_patch;
-  double *ws;          /* factorisation workspace: nws slots of ws_stride doubles */
+  double *ws;          /* factorisation workspace: a pool the class launches share        */
   double *kappa;       /* per-patch 1-norm condition estimates (nnodes), when cond_on    */
   int cond_on;
   /* per-particle adaptive Dormand-Prince (option dopri_per_particle): time reached, next step, step
@@ -139,8 +154,14 @@ typedef struct {
                           holding particles */
   double *tp, *hp, *hcur;
   int *active;
-  long long ws_stride;
-  int nws;
+  long long ws_stride; /* pool size (doubles) */
+  int nws;             /* CTAs of the largest class launch (0: no workspace) */
+  /* patch-size classes: work-list region (cls_off, nodes of the class: cls_cap), CTA size, grid
+     and workspace slot stride (doubles) of each class launch; cls_off_dev on the device */
+  int cls_off[LGB_NCLS + 1], cls_cap[LGB_NCLS], cls_threads[LGB_NCLS], cls_grid[LGB_NCLS];
+  long long cls_stride[LGB_NCLS];
+  int *cls_off_dev;
+  int factor_threads;  /* option factor_threads: one CTA size for every class (0: the table) */
   /* particle swarm */
   int np, np_cap;
   double *xp, *fields, *vel, *x0, *vadv;
