@@ -18,6 +18,7 @@ Legs:
 Run: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference] [--np NP]
 """
 import argparse
+import faulthandler
 import json
 import os
 import subprocess
@@ -29,6 +30,14 @@ import numpy as np
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
+
+T_START = time.perf_counter()
+
+
+def log(msg):
+    """Progress on stderr (the JSON result line alone goes to stdout)."""
+    print("[bench %7.1fs] %s" % (time.perf_counter() - T_START, msg), file=sys.stderr, flush=True)
+
 
 METRIC = "3D RK4 particle-steps/s (FP32 eval <=1e-6 vs FP64; plain FP64 alongside)"
 DT = 5e-4
@@ -204,7 +213,9 @@ def run_serving(njobs, workers=8, budget=150e9, sweep=(5.0, 10.0, 20.0, 40.0), s
                 for _, job in stream[:sweep_jobs]]
     rates = []
     sustainable = None
+    log("serving: stream done, rate sweep")
     for rate in sweep:
+        log("serving: %g jobs/s" % rate)
         arr = np.cumsum(np.random.default_rng(11).exponential(1.0 / rate, size=len(resident)))
         srv.reset_stats()
         w = play(list(zip(arr.tolist(), resident)))
@@ -237,6 +248,7 @@ def run_uneven(rk4_steps=3, dopri_steps=5, t_end=0.1, pp_budget_s=90.0):
                        "8M particles from the mixture, FP32 evaluation"}
     for scheme, name in ((2, "rk4"), (3, "dopri"), (3, "dopri_per_particle")):
         pp = name == "dopri_per_particle"
+        log("uneven: %s" % name)
         c = L.LagRBFCtx(**opts, advection=True, advection_scheme=scheme, advection_cfl=0.3, solve_method=1,
                         eval_precision="fp32", dt=DT, petsc_options={"dopri_rtol": 1e-6, "dopri_atol": 1e-9,
                                                                       "dopri_per_particle": pp})
@@ -290,6 +302,7 @@ def run_precision_stress(np_=1_000_000, eps_h=1.0):
     opts = dict(opts, shape_factor=opts["shape_factor"] * eps_h)
     res, kap = {}, None
     for prec in ("fp64", "fp32"):
+        log("precision stress: eps_h %g, %s" % (eps_h, prec))
         c = L.LagRBFCtx(**opts, solve_method=1, eval_precision=prec)
         if prec == "fp64":
             c.set_condition_estimates(True)
@@ -363,6 +376,7 @@ def relerr_stats(a, b):
 
 
 def main():
+    faulthandler.enable()
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
@@ -399,8 +413,10 @@ def main():
 
     import lagrbf_gb300 as L
     cf = L.load_cfuncs()
+    log("workload")
     xd, fd, xp, opts = workload(args, rank)
     npart = len(xp)
+    log("set-up: %d nodes, %d particles" % (len(xd), npart))
     ctx = L.LagRBFCtx(**opts, advection=True, advection_scheme=2, advection_cfl=0.3, dt=DT,
                       solve_method=args.solve_method,
                       eval_precision="fp32", cuda_device=local)
@@ -429,6 +445,7 @@ def main():
         ctx.synchronize()
         print(json.dumps({"profile_only": True, "setup_s": setup_s, "stats": ctx.stats()}))
         return 0
+    log("set-up done in %.1f s; warm-up" % setup_s)
     t = 0.0
     for _ in range(args.warmup):
         ctx.advect_resident(t, t + DT)
@@ -453,6 +470,7 @@ def main():
     ps_total = allsum(st["particle_steps"])
     value = ps_total / el_max
     launches = st["launches"]
+    log("timed loop: %.3g particle-steps/s" % value)
     # ---------------- roofline of the evaluation kernel (event-timed launches) ----------------
     ctx.reset_stats()
     ctx.set_profiling(True)
@@ -487,6 +505,7 @@ def main():
                           "eval_ms_per_launch": roofline["per_launch_ms"], "frac": roofline["frac"],
                           "chunk_cap": st["chunk_cap"], "records": st["records"], "np": npart}))
         return 0
+    log("FP32 vs FP64")
     # ---------------- FP32 vs FP64 error after one step from the same state ----------------
     def snapshot():
         x = np.zeros((npart, 3)); f = np.zeros((npart, 3)); p = np.zeros(npart, dtype=np.int64)
@@ -506,6 +525,7 @@ def main():
     err_max, err_rms = relerr_stats(f32, f64)
     err_pw = pointwise_relerr(f32, f64)
     pos_err = float(np.abs(x32 - x64).max())
+    log("FP64 steps")
     # ---------------- plain FP64 path throughput ----------------
     ctx.set_precision(False)
     ctx.reset_stats()
@@ -518,6 +538,7 @@ def main():
     el64 = allmax(time.perf_counter() - ts)
     value64 = allsum(ctx.stats()["particle_steps"]) / el64
     ctx.set_precision(True)
+    log("end to end")
     # ---------------- end to end through the reference-facing C-ABI, host buffers ----------------
     ke = args.e2e_steps or args.steps
     xo = np.zeros((npart, 3)); fo = np.zeros((npart, 3)); po = np.zeros(npart, dtype=np.int64)
@@ -559,22 +580,27 @@ def main():
     # ---------------- FP32 vs FP64 trajectories over 50 steps (1M-particle sample) ----------------
     trajectory = None
     if rank == 0 and world == 1 and args.serve_jobs > 0:
+        log("trajectories")
         trajectory = run_trajectory(xd, fd, xp[:1 << 20], opts)
     # ---------------- precision stress (Gaussian, small shape parameter) ----------------
     precision = None
     if rank == 0 and world == 1 and args.serve_jobs > 0:
+        log("precision stress")
         precision = run_precision_stress()
         precision["flattened"] = run_precision_stress(np_=250_000, eps_h=0.35)
     # ---------------- serving loop: Poisson stream of mixed advection jobs ----------------
     uneven = None
     if rank == 0 and world == 1 and args.uneven:
+        log("uneven")
         uneven = run_uneven()
     serve = None
     if rank == 0 and world == 1 and args.serve_jobs > 0:
+        log("serving")
         serve = run_serving(args.serve_jobs)
     # ---------------- CPU baseline on the host cores ----------------
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
+        log("CPU baseline")
         try:
             r, P = cpu_baseline(xd, fd, opts, args, 1)
             cpu = {"value": r["particle_steps"] / r["step_s"], "unit": "particle-steps/s", "cores": P, "kind": "port",

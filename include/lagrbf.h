@@ -274,7 +274,9 @@ LAGRBF_EXPORT void lagrbf_server_destroy(void *server);
    cell.  All scratch is a static device array of this library sized for at most
    LAGRBF_NOALLOC_MAX_CELLS cells; larger meshes are rejected with LAGRBF_ERR_ARG_OUTOFRANGE.
    Asynchronous on `stream` (cudaStream_t, NULL = legacy default stream).  The first call on a device
-   (that device current) resolves the scratch address, so it should precede any stream capture.
+   (that device current) resolves the scratch address, so it should precede any stream capture; the
+   address is kept for the life of the process, so the entry point must not be used after
+   cudaDeviceReset or from a context other than the device's primary context.
    Calls that overlap on one device share the scratch and race: keep them on one stream. */
 #define LAGRBF_NOALLOC_MAX_CELLS (1 << 20)
 LAGRBF_EXPORT int lagrbf_gpu_bin_points_noalloc(int32_t dim, const int32_t *nodes, const double *O, const double *L,

@@ -195,7 +195,9 @@ static int na_fail(int code, const char *what, cudaError_t e)
   return lgb_set_error_msg(code, msg);
 }
 
-/* Scratch address on the current device, resolved once per device. */
+/* Scratch address on the current device, resolved once per device and kept for the life of the
+   process: after cudaDeviceReset, or in a context other than the device's primary context, the
+   kept address is stale and the entry point must not be used. */
 static int na_scratch(int **ptr)
 {
   int dev = -1;

@@ -140,5 +140,17 @@ def test_noalloc_rejects_meshes_beyond_scratch():
     rc = f(3, nodes, O, Lb, 0, None, None, start.ctypes.data, None, None)
     assert rc == 63
     assert "static scratch" in _lib.last_error()
-    cells = 1025 * 1025
-    assert cells > MAX_CELLS
+
+
+def test_noalloc_accepts_the_largest_mesh():
+    """Exactly LAGRBF_NOALLOC_MAX_CELLS cells (2D, 1025 x 1025 nodes): accepted, binned like the
+    floor((x - O) / h) convention on a few points, corners and the upper face included."""
+    torch = pytest.importorskip("torch")
+    nodes = (1025, 1025)
+    assert (nodes[0] - 1) * (nodes[1] - 1) == MAX_CELLS
+    x = np.array([[0.0, 0.0], [1.0, 1.0], [0.5, 0.25], [0.999, 0.001], [0.1234, 0.9876]])
+    cid, start, order = _bin_noalloc(torch, 2, nodes, x)
+    t = np.minimum(np.floor(x * 1024).astype(np.int64), 1023)
+    assert np.array_equal(cid, t[:, 0] + 1024 * t[:, 1])
+    assert start[-1] == len(x) and len(start) == MAX_CELLS + 1
+    assert np.array_equal(np.sort(order), np.arange(len(x)))
