@@ -160,7 +160,9 @@ LAGRBF_EXPORT int lagrbf_gpu_get_condition(void *ctx, double *kappa, double *sum
    option setup_all_patches and a completed interpolation (every patch set up and solved), so that
    nothing ctx does writes the shared state; lagrbf_fill_swarm of the data on ctx is refused and its
    coefficient reset does nothing.  The owner must outlive ctx and keep its data unchanged while ctx
-   is in use. */
+   is in use.  The call does not touch the owner's stream, so the owner's thread may go on
+   advecting its own particles meanwhile (its interpolation must have returned before this call,
+   ordered by the caller's own thread synchronisation). */
 LAGRBF_EXPORT int lagrbf_gpu_share_dataset(void *ctx, void *owner);
 /* Coupling of sharded runs (one process and GPU per rank, each holding the whole dataset and a pid
    range of the particles): fn(vals, n, user) must replace vals[0..n) by their element-wise maximum

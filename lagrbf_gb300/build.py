@@ -66,7 +66,7 @@ def build(verbose=False, force=False):
         o = os.path.join(BUILD, src + ".o")
         objs.append(o)
         if force or _stale(o, [s] + headers):
-            jobs.append(["gcc", "-std=gnu11", "-O3", "-fPIC", "-Wall", "-Wextra", "-Wno-unused-parameter",
+            jobs.append(["gcc", "-std=gnu11", "-O3", "-g", "-fPIC", "-Wall", "-Wextra", "-Wno-unused-parameter",
                          "-ffp-contract=off", "-fvisibility=hidden", "-I" + os.path.join(cuda, "include"),
                          "-c", s, "-o", o])
     if jobs:

@@ -1305,6 +1305,10 @@ static int run_interval_on_device(lgb_ctx *c, int analytical, int *rc)
         int r = step_sequence(c, analytical);
         if (!r) r = lgb_op_loop_cond(&c->d, (unsigned long long)h, c->stream);
         ok = (cudaStreamEndCapture(c->stream, &body) == cudaSuccess) && !r;
+        /* a capture into the conditional body that failed leaves that body in no defined state:
+           destroying the parent graph then crashed the driver, so this one graph is left alone
+           (once per context: the device loop is off from then on) */
+        if (!ok) g = NULL;
       }
     }
     c->wgraph_eval_launches = c->eval_launches - e0;
@@ -1688,7 +1692,9 @@ LAGRBF_EXPORT int lagrbf_gpu_share_dataset(void *ctx, void *owner)
   for (k = 0; k < 3; k++)
     if (d->g.n[k] != o->d.g.n[k] || d->g.O[k] != o->d.g.O[k] || d->g.L[k] != o->d.g.L[k])
       return set_error(LAGRBF_ERR_ARG_WRONG, "dataset sharing: different PU mesh");
-  CU(cudaStreamSynchronize(o->stream));
+  /* The owner's stream is not synchronised here: all_ready is set only after the owner's
+     interpolation has drained that stream, and the owner's thread may be capturing a graph on it
+     right now (a synchronisation from this thread would invalidate that capture). */
   CU(cudaStreamSynchronize(c->stream));
   free_data(d);
   DFREE(d->cstart); DFREE(d->pm); DFREE(d->slot); DFREE(d->setup); DFREE(d->solved);

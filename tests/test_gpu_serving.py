@@ -89,3 +89,68 @@ def test_shared_dataset_gives_the_owners_values():
     del other
     owner.fill_points(xp[:5], pidx=pid[:5])
     owner.interpolate_c()  # the owner is unaffected by the sharing context's teardown
+
+
+def test_sharing_while_the_owner_captures_its_step_loop():
+    """Contexts share a dataset while the owner's thread keeps advecting its own particles: the
+    owner's precision is switched before every interval, which drops its graphs, so each interval
+    is captured again as a device-side step loop and sharing often falls inside that capture.
+    Sharing must leave the owner's stream alone; every sharer's positions equal those of a sharer
+    run before the race, bit for bit, and the owner's run completes."""
+    import threading
+    import lagrbf_gb300 as L
+    xd, fd, npu = _datasets()[0]
+    opts = dict(dim=3, npartitions=[npu] * 3, overlap=W.pu_overlap(npu), shape_factor=1.0, kernel=2, nfields=3,
+                advection=True, advection_scheme=2, advection_cfl=0.3, dt=2e-3, eval_precision="fp32",
+                petsc_options={"setup_all_patches": True})
+    rng = np.random.default_rng(21)
+    xo = 0.2 + 0.6 * rng.uniform(0, 1, (3000, 3))
+    xq = 0.2 + 0.6 * rng.uniform(0, 1, (1500, 3))
+    pq = np.arange(1, len(xq) + 1, dtype=np.int64)
+    owner = L.LagRBFCtx(**opts)
+    owner.fill_data(xd, fd)
+    owner.fill_points(xo, pidx=np.arange(1, len(xo) + 1, dtype=np.int64))
+    owner.interpolate_c()
+    owner.synchronize()
+
+    def sharer_run():
+        s = L.LagRBFCtx(**opts)
+        s.share_dataset(owner)
+        s.fill_points(xq, pidx=pq)
+        s.interpolate_c()
+        s.advect_resident(0.0, 4e-3)
+        x = np.zeros((len(xq), 3))
+        s.output(coords=x)
+        del s
+        return x
+
+    expect = sharer_run()
+    errors, results = [], []
+    stop = threading.Event()
+
+    def owner_loop():
+        try:
+            t, k = 0.0, 0
+            while not stop.is_set() and k < 400:
+                owner.set_precision(k % 2 == 0)
+                owner.advect_resident(t, t + 2e-3)
+                t += 2e-3
+                k += 1
+        except Exception as e:  # reported below
+            errors.append(e)
+
+    th = threading.Thread(target=owner_loop)
+    th.start()
+    try:
+        for _ in range(30):
+            results.append(sharer_run())
+    except Exception as e:
+        errors.append(e)
+    finally:
+        stop.set()
+        th.join()
+    assert not errors, errors
+    assert len(results) == 30
+    for x in results:
+        assert np.array_equal(x, expect)
+    assert np.abs(expect).sum() > 0
