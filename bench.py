@@ -62,6 +62,9 @@ def parse():
                     help="setup, reset_coefficients, one re-solve of every patch (kept factors), for ncu")
     ap.add_argument("--serve-jobs", type=int, default=60, help="jobs of the serving leg (0: skip it)")
     ap.add_argument("--uneven", type=int, default=1, help="run the uneven-mixture leg (0: skip it)")
+    ap.add_argument("--device-loop", type=int, default=1,
+                    help="0: one graph launch per internal step instead of the device-side step loop "
+                         "(ncu does not profile kernels inside graphs with conditional nodes)")
     ap.add_argument("--solve-method", type=int, default=1,
                     help="1: A_KSP (factors resident), 2: A_KSP_ASMB (re-factor, no factor storage)")
     return ap.parse_args()
@@ -419,7 +422,7 @@ def main():
     log("set-up: %d nodes, %d particles" % (len(xd), npart))
     ctx = L.LagRBFCtx(**opts, advection=True, advection_scheme=2, advection_cfl=0.3, dt=DT,
                       solve_method=args.solve_method,
-                      eval_precision="fp32", cuda_device=local)
+                      eval_precision="fp32", cuda_device=local, device_loop=bool(args.device_loop))
     # ---------------- setup (not timed in `value`) ----------------
     t0 = time.perf_counter()
     ctx.fill_data(xd, fd)
@@ -492,7 +495,7 @@ def main():
                 "traffic_source": ("ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch on a smaller "
                                    "case with the same per-cell densities, per particle, times this launch's "
                                    "particles (%s)" % tsrc) if tsrc else None,
-                "kernel": "k_eval<float,3,3,2,KER_C2> (PU evaluation)",
+                "kernel": "k_eval_rec<3,3,KER_C2> (PU evaluation from TMA-streamed record blocks)",
                 "peak_source": "measured: FFMA-chain probe on this GPU in this run (lagrbf_gpu_fp32_peak_tflops)",
                 "per_launch_ms": sp["eval_ms"] / max(sp["eval_launches"], 1),
                 "flops_per_launch": sp["eval_flops"] / max(sp["eval_launches"], 1),
@@ -537,6 +540,22 @@ def main():
     ctx.synchronize()
     el64 = allmax(time.perf_counter() - ts)
     value64 = allsum(ctx.stats()["particle_steps"]) / el64
+    # the FP64 evaluation kernel against the FP64 pipe (event-timed launches of one profiled step)
+    ctx.reset_stats()
+    ctx.set_profiling(True)
+    ctx.advect_resident(t, t + DT)
+    t += DT
+    ctx.synchronize()
+    sp64 = ctx.stats()
+    ctx.set_profiling(False)
+    fp64_peak = cf["lagrbf_gpu_fp64_peak_tflops"]()
+    e64 = sp64["eval_flops"] / (sp64["eval_ms"] * 1e-3) / 1e12 if sp64["eval_ms"] > 0 else 0.0
+    roofline64 = {"bound": "fp64", "achieved": e64, "peak": fp64_peak, "unit": "TFLOP/s",
+                  "frac": e64 / fp64_peak if fp64_peak > 0 else None,
+                  "kernel": "k_eval<double,3,3,1,KER_GENERIC> (PU evaluation, FP64 gather path)",
+                  "peak_source": "measured: DFMA-chain probe on this GPU in this run (lagrbf_gpu_fp64_peak_tflops)",
+                  "per_launch_ms": sp64["eval_ms"] / max(sp64["eval_launches"], 1),
+                  "flops_per_launch": sp64["eval_flops"] / max(sp64["eval_launches"], 1)}
     ctx.set_precision(True)
     log("end to end")
     # ---------------- end to end through the reference-facing C-ABI, host buffers ----------------
@@ -624,7 +643,7 @@ def main():
                        "setup_s": setup_s, "patches_factored": st0["patches_factored"],
                        "max_patch": st0["max_patch"], "work_unit": st["chunk_cap"],
                        "staging": "TMA bulk copies of precomputed record blocks" if st["records"] else "gather"},
-            "fp64": {"value": value64, "unit": "particle-steps/s", "steps": args.fp64_steps,
+            "fp64": {"value": value64, "unit": "particle-steps/s", "steps": args.fp64_steps, "roofline": roofline64,
                      "fp32_speedup": value / value64 if value64 > 0 else None,
                      "fp32_vs_fp64_max_rel_err": err_max, "fp32_vs_fp64_rms_rel_err": err_rms,
                      "fp32_vs_fp64_pointwise_rel_err": err_pw, "fp32_vs_fp64_max_abs_pos_err": pos_err,

@@ -90,7 +90,10 @@ LAGRBF_EXPORT void lagrbf_interpolate_driver(int32_t ndata_local, double *data_c
    pu_mesh_shape_factor, n_interpolation_fields, kernel_type, solve_method, advection,
    advection_scheme, velocity_name, dt, cfl_fac, rmin, rmax, dopri_dt_fac, dopri_dt_fac_min,
    dopri_dt_fac_max, dopri_atol, dopri_rtol; and the GPU-only keys eval_precision (fp64|fp32,
-   default fp64), use_cuda_graph (bool, default true), cuda_device (int), output_direct (bool,
+   default fp64), use_cuda_graph (bool, default true), device_loop (bool, default true: an
+   advection interval runs as one graph launch whose step is the body of a device-side while loop;
+   false keeps one graph launch per internal step, whose kernels profilers can attribute),
+   cuda_device (int), output_direct (bool,
    default true: when the device accesses pageable host memory, lagrbf_output's particle rows are
    written by the GPU straight into the caller's arrays and lagrbf_fill_swarm's data arrays are
    read by it directly), dopri_per_particle (bool, default false: per-particle adaptive
@@ -147,6 +150,8 @@ LAGRBF_EXPORT int lagrbf_gpu_set_precision(void *ctx, int fp32);
 /* FP32 FMA throughput of the current device in TFLOP/s, measured by a synthetic kernel
    (dependent FFMA chains, all SMs): the FP32 roofline denominator. */
 LAGRBF_EXPORT double lagrbf_gpu_fp32_peak_tflops(void);
+/* The same for FP64 (dependent DFMA chains): the FP64 roofline denominator. */
+LAGRBF_EXPORT double lagrbf_gpu_fp64_peak_tflops(void);
 /* Per-patch condition estimates: while on, every patch factorisation also estimates
    kappa_1(A) = ||A||_1 ||A^-1||_1 of its collocation matrix (||A^-1||_1 by Hager's method as refined
    by Higham, a few extra triangular solves per patch; the factorisation itself is unchanged).

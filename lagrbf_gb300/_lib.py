@@ -111,6 +111,7 @@ def register_functions(clib):
     reg("lagrbf_output_files", ctypes.c_int, [ctypes.c_void_p, ctypes.c_bool, ctypes.c_int32, ctypes.c_char_p,
                                               ctypes.c_char_p])
     reg("lagrbf_gpu_fp32_peak_tflops", ctypes.c_double, [])
+    reg("lagrbf_gpu_fp64_peak_tflops", ctypes.c_double, [])
     reg("lagrbf_gpu_get_stats", ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Stats)])
     reg("lagrbf_gpu_reset_stats", ctypes.c_int, [ctypes.c_void_p])
     reg("lagrbf_gpu_synchronize", ctypes.c_int, [ctypes.c_void_p])

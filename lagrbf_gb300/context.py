@@ -84,6 +84,7 @@ class LagRBFCtx:
         o["rmax"] = kwargs.get("rmax", o.getReal("rmax", 1e132))
         o["eval_precision"] = kwargs.get("eval_precision", o.getString("eval_precision", "fp64"))
         o["use_cuda_graph"] = kwargs.get("use_cuda_graph", o.getBool("use_cuda_graph", True))
+        o["device_loop"] = kwargs.get("device_loop", o.getBool("device_loop", True))
         o["output_direct"] = kwargs.get("output_direct", o.getBool("output_direct", True))
         if "cuda_device" in kwargs or "cuda_device" in o:
             o["cuda_device"] = int(kwargs.get("cuda_device", o.get("cuda_device", 0)))

@@ -13,7 +13,8 @@ extern "C" int lgb_build_records_2d(const EvalParams *P, int force, int grid, vo
 
 /* Staging budgets (elements): FP32 gather 30 KB, FP32 record stream 4 stages x 4 KB, FP64 48 KB. */
 #define BUDGET32 7680
-#define BUDGET32_TMA 1024
+#include "lgb_eval_tune.h"
+#define BUDGET32_TMA LGB_TMA_BUDGET_TUNED /* floats per staging round of the record kernel */
 #define BUDGET64 6144
 /* Polls of a bounded mbarrier wait of the evaluation kernel before it reports a timeout. */
 #define EVAL_POLL_LIMIT (1 << 22)
@@ -43,6 +44,8 @@ static int launch64_fp(const EvalParams &P, int fp, int grid, cudaStream_t s)
   }
 }
 
+/* Floats per staging round: the measured table's value; LAGRBF_TMA_BUDGET overrides it for the
+   tuner (lagrbf_gb300/tune_eval.py), which times every candidate without a rebuild. */
 static int tma_budget(void)
 {
   static int b = -1;

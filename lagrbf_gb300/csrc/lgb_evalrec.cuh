@@ -50,7 +50,10 @@ __host__ __device__ __forceinline__ double evr_scale(const lgb_geom &g)
   return g.kernel == LGB_KERNEL_GAUSSIAN ? 1.0 : g.eps_r;
 }
 
-#define EVR_NB 4 /* stages in the ring */
+#include "lgb_eval_tune.h"
+#ifndef EVR_NB
+#define EVR_NB LGB_EVR_NB_TUNED /* stages in the ring (measured table) */
+#endif
 #ifndef LGB_EVR_UNROLL
 #define LGB_EVR_UNROLL 4 /* points of a segment in flight per thread */
 #endif

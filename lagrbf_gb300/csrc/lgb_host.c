@@ -234,7 +234,7 @@ typedef struct lgb_ctx_s {
   lgb_dev d;
   cudaStream_t stream;
   /* configuration (LagRBFSetFromOptions) */
-  int advection, scheme, use_graph;
+  int advection, scheme, use_graph, device_loop;
   double dt0, cfl_fac, rmin, rmax;
   double dopri[5];
   /* host mirrors */
@@ -520,6 +520,8 @@ static int read_options(lgb_ctx *c)
   }
   c->use_graph = 1;
   opt_bool("use_cuda_graph", &c->use_graph);
+  c->device_loop = 1;
+  opt_bool("device_loop", &c->device_loop);
   c->out_direct = 1;
   opt_bool("output_direct", &c->out_direct);
   return 0;
@@ -1279,7 +1281,9 @@ static int run_interval_on_device(lgb_ctx *c, int analytical, int *rc)
 {
   long long s0;
   *rc = 0;
-  if (!c->use_graph || c->profiling || c->reduce || (analytical && !c->d.vfield) || c->wgraph_failed) return 0;
+  if (!c->use_graph || !c->device_loop || c->profiling || c->reduce || (analytical && !c->d.vfield) ||
+      c->wgraph_failed)
+    return 0;
   if (c->wgraph_valid && c->wgraph_mode != analytical) invalidate_graph(c);
   if (!c->wgraph_valid) {
     cudaGraph_t g = NULL, body;
@@ -1626,6 +1630,8 @@ LAGRBF_EXPORT int lagrbf_gpu_advect_resident(void *ctx, double time, double time
 
 double lgb_fp32_peak_tflops(void);
 LAGRBF_EXPORT double lagrbf_gpu_fp32_peak_tflops(void) { return lgb_fp32_peak_tflops(); }
+double lgb_fp64_peak_tflops(void);
+LAGRBF_EXPORT double lagrbf_gpu_fp64_peak_tflops(void) { return lgb_fp64_peak_tflops(); }
 
 LAGRBF_EXPORT int lagrbf_gpu_set_velocity_field(void *ctx, int32_t kind, const double *params, int32_t nparams)
 {

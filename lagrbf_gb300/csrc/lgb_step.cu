@@ -517,36 +517,39 @@ extern "C" int lgb_op_ctrl(lgb_dev *d, int what, void *stream)
   return (int)cudaGetLastError();
 }
 
-/* FP32 FMA throughput probe: 8 independent dependent-FFMA chains per thread, 2 flops each. */
-__global__ void k_ffma(float *out, int iters, float a, float b)
+/* FMA throughput probe (FP32 or FP64): 8 independent dependent-FMA chains per thread, 2 flops each. */
+template <typename T>
+__global__ void k_fma_probe(T *out, int iters, T a, T b)
 {
-  float x0 = threadIdx.x, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3, x4 = x0 + 4, x5 = x0 + 5, x6 = x0 + 6, x7 = x0 + 7;
+  T x0 = threadIdx.x, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3, x4 = x0 + 4, x5 = x0 + 5, x6 = x0 + 6, x7 = x0 + 7;
   for (int i = 0; i < iters; i++) {
 #pragma unroll
     for (int u = 0; u < 16; u++) {
-      x0 = fmaf(x0, a, b); x1 = fmaf(x1, a, b); x2 = fmaf(x2, a, b); x3 = fmaf(x3, a, b);
-      x4 = fmaf(x4, a, b); x5 = fmaf(x5, a, b); x6 = fmaf(x6, a, b); x7 = fmaf(x7, a, b);
+      x0 = fma(x0, a, b); x1 = fma(x1, a, b); x2 = fma(x2, a, b); x3 = fma(x3, a, b);
+      x4 = fma(x4, a, b); x5 = fma(x5, a, b); x6 = fma(x6, a, b); x7 = fma(x7, a, b);
     }
   }
-  float s = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
-  if (s == 1234.5f) out[0] = s; /* keep the chains alive */
+  T s = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
+  if (s == (T)1234.5) out[0] = s; /* keep the chains alive */
 }
 
-extern "C" double lgb_fp32_peak_tflops(void)
+/* Best of five event-timed launches of the probe over 4 CTAs of 512 threads per SM, in TFLOP/s. */
+template <typename T>
+static double fma_peak_tflops(int iters)
 {
   int nsm = 0, smem = 0;
   if (lgb_device_info(&nsm, &smem)) return -1.0;
-  float *out = NULL;
-  if (cudaMalloc(&out, sizeof(float)) != cudaSuccess) return -1.0;
-  const int threads = 512, blocks = nsm * 4, iters = 4096;
+  T *out = NULL;
+  if (cudaMalloc(&out, sizeof(T)) != cudaSuccess) return -1.0;
+  const int threads = 512, blocks = nsm * 4;
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
-  k_ffma<<<blocks, threads>>>(out, 64, 0.999f, 0.001f); /* warm-up */
+  k_fma_probe<T><<<blocks, threads>>>(out, 16, (T)0.999, (T)0.001); /* warm-up */
   float best = 1e30f;
   for (int r = 0; r < 5; r++) {
     cudaEventRecord(e0);
-    k_ffma<<<blocks, threads>>>(out, iters, 0.999f, 0.001f);
+    k_fma_probe<T><<<blocks, threads>>>(out, iters, (T)0.999, (T)0.001);
     cudaEventRecord(e1);
     cudaEventSynchronize(e1);
     float ms = 0.f;
@@ -561,3 +564,6 @@ extern "C" double lgb_fp32_peak_tflops(void)
   double flops = 2.0 * 8 * 16 * (double)iters * threads * blocks;
   return flops / (best * 1e-3) / 1e12;
 }
+
+extern "C" double lgb_fp32_peak_tflops(void) { return fma_peak_tflops<float>(4096); }
+extern "C" double lgb_fp64_peak_tflops(void) { return fma_peak_tflops<double>(256); }

@@ -109,6 +109,8 @@ def test_create_without_gpu_fails_cleanly(lib):
     assert b"CUDA" in lib.lagrbf_gpu_last_error()
     lib.lagrbf_gpu_fp32_peak_tflops.restype = ctypes.c_double
     assert lib.lagrbf_gpu_fp32_peak_tflops() < 0
+    lib.lagrbf_gpu_fp64_peak_tflops.restype = ctypes.c_double
+    assert lib.lagrbf_gpu_fp64_peak_tflops() < 0
 
 
 def test_create_rejects_bad_options(lib):
