@@ -489,6 +489,32 @@ def test_uneven_mixture_matches_oracle(scheme):
         assert abs(c.stats()["dt"] - o.dt()) <= 1e-9 * abs(o.dt())
 
 
+def test_uneven_mixture_per_particle_dopri_matches_oracle():
+    """Per-particle Dormand-Prince (option dopri_per_particle) on the uneven mixture, where particles
+    in dense clusters and in sparse cells need very different steps: the GPU and the oracle take the
+    same sweeps, accept the same particle steps and end at the same positions."""
+    xd, fd, xp, opts = W.config_uneven_3d(nd=10000, npu=24, np_=15000, seed=5)
+    adv = dict(advection=True, advection_scheme=3, advection_cfl=0.3, solve_method=1)
+    c = gpu_ctx(opts, **adv, petsc_options={"dopri_per_particle": True, "dopri_rtol": 1e-6, "dopri_atol": 1e-9})
+    o = Oracle(**opts, **adv, dopri_per_particle=True, dopri_rtol=1e-6, dopri_atol=1e-9)
+    c.fill_points(xp)
+    assert o.fill(False, xp) == 0
+    t, dt = 0.0, 5e-3
+    for _ in range(2):
+        c.fill_data(xd, fd); c.interpolate_c()
+        assert o.fill(True, xd, fd) == 0 and o.interpolate() == 0
+        c.advect_interpolate_c(t, t + dt)
+        assert o.advect(t, t + dt) == 0
+        t += dt
+    x1, _, p1 = gpu_output(c, len(xp), 3)
+    x2, _, p2 = o.output(len(xp))
+    assert np.array_equal(p1, p2)
+    st = c.stats()
+    assert st["steps"] == o.counts()[3]
+    assert st["particle_steps"] == o.accepted()
+    assert np.abs(x1 - x2).max() <= 1e-11
+
+
 @pytest.mark.parametrize("dim,n,O,L", [(3, 32, 0.0, 1.0), (3, 7, -0.3, 1.7), (2, 13, -2.0, -0.5), (2, 160, 0.0, 1.0),
                                        (3, 9, -1.0, 1.0)])
 def test_locate_at_cell_faces(dim, n, O, L):
