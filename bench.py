@@ -62,6 +62,8 @@ def parse():
                     help="setup, reset_coefficients, one re-solve of every patch (kept factors), for ncu")
     ap.add_argument("--serve-jobs", type=int, default=60, help="jobs of the serving leg (0: skip it)")
     ap.add_argument("--uneven", type=int, default=1, help="run the uneven-mixture leg (0: skip it)")
+    ap.add_argument("--eval-precision", default="fp32", choices=["fp32", "fp64"],
+                    help="evaluation precision of the main context (fp64: the plain path, for profiling it)")
     ap.add_argument("--device-loop", type=int, default=1,
                     help="0: one graph launch per internal step instead of the device-side step loop "
                          "(ncu does not profile kernels inside graphs with conditional nodes)")
@@ -422,7 +424,7 @@ def main():
     log("set-up: %d nodes, %d particles" % (len(xd), npart))
     ctx = L.LagRBFCtx(**opts, advection=True, advection_scheme=2, advection_cfl=0.3, dt=DT,
                       solve_method=args.solve_method,
-                      eval_precision="fp32", cuda_device=local, device_loop=bool(args.device_loop))
+                      eval_precision=args.eval_precision, cuda_device=local, device_loop=bool(args.device_loop))
     # ---------------- setup (not timed in `value`) ----------------
     t0 = time.perf_counter()
     ctx.fill_data(xd, fd)

@@ -159,3 +159,20 @@ def test_python_surface_mirrors_lagrbfpy():
                 if name in deprecated:
                     continue
                 assert hasattr(ours, name), (cls.name, fn.name)
+
+
+def test_record_loop_probe_compiles(tmp_path):
+    """The compute-only probe of the evaluation's record loop (lagrbf_gb300/probe_eval.py) builds for
+    sm_103a (it runs only on a GPU)."""
+    import subprocess
+    from lagrbf_gb300 import build
+    try:
+        cuda = build._cuda_home()
+    except RuntimeError:
+        pytest.skip("nvcc not available")
+    src = os.path.join(os.path.dirname(build.__file__), "csrc", "probe_record_loop.cu")
+    out = tmp_path / "probe.o"
+    r = subprocess.run([os.path.join(cuda, "bin", "nvcc"), "-std=c++17", *build.ARCH, "-c", src, "-o", str(out)],
+                       stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+    assert r.returncode == 0, r.stdout
+    assert out.exists()
