@@ -1985,18 +1985,21 @@ int lgb_ctx_dims(void *ctx, int *dim, int *nfields)
   return 0;
 }
 
-/* Scheme and initial step of an existing context (the serving loop runs jobs with different RK
-   orders on one resident dataset). */
-int lgb_ctx_set_scheme(void *ctx, int scheme, double dt)
+/* Scheme, initial step and CFL factor of an existing context (the serving loop runs jobs with
+   different RK orders and steps on one resident dataset, and reuses contexts between jobs). */
+int lgb_ctx_set_scheme(void *ctx, int scheme, double dt, double cfl)
 {
   lgb_ctx *c = (lgb_ctx *)ctx;
   if (!c) return set_error(LAGRBF_ERR_ARG_NULL, "context is NULL");
   if (scheme < 0 || scheme > 3) return set_error(LAGRBF_ERR_ARG_OUTOFRANGE, "unknown advection scheme %d", scheme);
+  if (!(cfl > 0.0)) return set_error(LAGRBF_ERR_ARG_OUTOFRANGE, "CFL factor must be positive");
   CU(cudaMemcpyAsync(c->hctrl, c->d.ctrl, sizeof(lgb_ctrl), cudaMemcpyDeviceToHost, c->stream));
   CU(cudaStreamSynchronize(c->stream));
   c->scheme = scheme;
   c->dt0 = dt;
+  c->cfl_fac = cfl;
   c->hctrl->scheme = scheme;
+  c->hctrl->cfl_fac = cfl;
   c->hctrl->dt_adv = dt;
   c->hctrl->dopri_error = DBL_MAX;
   CU(cudaMemcpyAsync(c->d.ctrl, c->hctrl, sizeof(lgb_ctrl), cudaMemcpyHostToDevice, c->stream));

@@ -26,10 +26,14 @@
 #include <time.h>
 
 int lgb_set_error_msg(int code, const char *msg);
-int lgb_ctx_set_scheme(void *ctx, int scheme, double dt);
+int lgb_ctx_set_scheme(void *ctx, int scheme, double dt, double cfl);
 
 /* Device bytes of a context that shares a resident dataset, beyond its particles. */
 #define SHARE_BYTES (64LL << 20)
+/* Sharing contexts kept per resident dataset between jobs: a later job on the dataset reuses one
+   instead of creating a context (allocations) and destroying it (cudaFree synchronises the whole
+   device, so every job's teardown would wait for the other workers' kernels). */
+#define SRV_IDLE_MAX 8
 
 typedef struct srv_job {
   int64_t id;
@@ -50,9 +54,12 @@ typedef struct {
   int busy;               /* the owner context runs a job                                    */
   int ready;              /* every patch set up and solved: other jobs may share the dataset */
   int users;              /* running jobs on the dataset (owner and sharing contexts)        */
-  long long bytes;        /* estimate held by this context */
+  long long bytes;        /* estimate held by the owner context and the idle sharing contexts */
   int np_cap;
   double last_used;
+  void *idle[SRV_IDLE_MAX];            /* idle contexts sharing this dataset, ready for reuse */
+  long long idle_bytes[SRV_IDLE_MAX];  /* the device-memory estimate each of them holds    */
+  int nidle;
 } srv_dataset;
 
 typedef struct {
@@ -115,6 +122,8 @@ static srv_dataset *find_ds(srv_t *s, int64_t id)
 
 static void drop_ds(srv_t *s, int i)
 {
+  int k;
+  for (k = 0; k < s->ds[i].nidle; k++) lagrbf_destroy(s->ds[i].idle[k]); /* they borrow the owner's arrays */
   if (s->ds[i].ctx) lagrbf_destroy(s->ds[i].ctx);
   s->in_use -= s->ds[i].bytes;
   s->ds[i] = s->ds[--s->nds];
@@ -124,7 +133,11 @@ static void drop_ds(srv_t *s, int i)
 static long long job_extra(srv_t *s, const srv_job *j)
 {
   srv_dataset *d = find_ds(s, j->spec.dataset_id);
-  if (d && d->busy) return particle_bytes(&j->spec) + SHARE_BYTES; /* a context sharing the dataset */
+  if (d && d->busy) { /* a context sharing the dataset: an idle one is reused, growing if needed */
+    const long long need = particle_bytes(&j->spec) + SHARE_BYTES;
+    const long long held = d->nidle > 0 ? d->idle_bytes[d->nidle - 1] : 0;
+    return need > held ? need - held : 0;
+  }
   if (d) return (j->spec.np > d->np_cap) ? pbytes(j->spec.np, j->spec.dim) - pbytes(d->np_cap, j->spec.dim) : 0;
   return dataset_bytes(&j->spec) + particle_bytes(&j->spec);
 }
@@ -242,7 +255,7 @@ static int run_job(srv_t *s, void *ctx, srv_job *j, int fill, int owner)
   int rc = 0, k;
   double t = 0.0;
   if (fill && (rc = lagrbf_fill_swarm(ctx, true, p->nd, j->xd, j->fd, NULL))) return rc;
-  if ((rc = lgb_ctx_set_scheme(ctx, p->scheme, p->dt))) return rc;
+  if ((rc = lgb_ctx_set_scheme(ctx, p->scheme, p->dt, p->cfl > 0 ? p->cfl : 0.3))) return rc;
   if ((rc = lagrbf_gpu_set_precision(ctx, p->fp32))) return rc;
   pid = (int64_t *)malloc(sizeof(int64_t) * (size_t)(p->np > 0 ? p->np : 1));
   if (!pid) return lgb_set_error_msg(LAGRBF_ERR_MEM, "out of host memory");
@@ -267,21 +280,29 @@ static void *worker(void *arg)
   for (;;) {
     srv_job *j = NULL;
     srv_dataset *d;
-    void *ctx = NULL, *share = NULL;
+    void *ctx = NULL, *share = NULL, *reuse = NULL;
     int fill = 0, cached, rc, owner = 0;
-    long long extra;
+    long long extra, ctx_bytes;
     while (!s->stop && !(j = pick(s))) pthread_cond_wait(&s->cv_work, &s->lock);
     if (!j) break;
     j->state = 1;
     j->t_start = now_s();
     extra = job_extra(s, j);
     s->in_use += extra;
+    ctx_bytes = extra;
     d = find_ds(s, j->spec.dataset_id);
     cached = j->spec.dataset_id > 0;
     if (d && d->busy) {
-      /* the owner context is running: share its dataset from a context of this job */
+      /* the owner context is running: share its dataset from a context of this job (an idle one
+         left by an earlier job if there is one; its bytes move from the dataset to this job) */
       d->users++;
       share = d->ctx;
+      if (d->nidle > 0) {
+        d->nidle--;
+        reuse = d->idle[d->nidle];
+        ctx_bytes += d->idle_bytes[d->nidle];
+        d->bytes -= d->idle_bytes[d->nidle];
+      }
     } else if (d) {
       d->busy = 1;
       d->users++;
@@ -310,7 +331,9 @@ static void *worker(void *arg)
     pthread_mutex_unlock(&s->lock);
 
     rc = 0;
-    if (share) {
+    if (reuse) {
+      ctx = reuse; /* already shares this dataset */
+    } else if (share) {
       ctx = create_job_ctx(s, &j->spec);
       rc = ctx ? lagrbf_gpu_share_dataset(ctx, share) : LAGRBF_ERR_GPU;
     } else if (!ctx) {
@@ -336,9 +359,18 @@ static void *worker(void *arg)
       d->last_used = now_s();
       if (rc && d->users == 0) drop_ds(s, (int)(d - s->ds)); /* a failed context is not reused */
       else if (rc) d->ready = 0;
+    } else if (d && share && ctx && !rc && !s->stop && d->nidle < SRV_IDLE_MAX) {
+      /* keep the sharing context for the next job on this dataset; its bytes stay in use, held by
+         the dataset (an eviction frees them with it) */
+      d->idle[d->nidle] = ctx;
+      d->idle_bytes[d->nidle] = ctx_bytes;
+      d->nidle++;
+      d->bytes += ctx_bytes;
+      d->users--;
+      d->last_used = now_s();
     } else {
       if (ctx) lagrbf_destroy(ctx);
-      s->in_use -= extra;
+      s->in_use -= ctx_bytes;
       if (d && share) {
         d->users--;
         d->last_used = now_s();
@@ -574,8 +606,7 @@ LAGRBF_EXPORT void lagrbf_server_destroy(void *srv)
   pthread_cond_broadcast(&s->cv_done);
   pthread_mutex_unlock(&s->lock);
   for (i = 0; i < s->nworkers; i++) pthread_join(s->threads[i], NULL);
-  for (i = 0; i < s->nds; i++)
-    if (s->ds[i].ctx) lagrbf_destroy(s->ds[i].ctx);
+  while (s->nds > 0) drop_ds(s, s->nds - 1); /* sharing contexts before their owner */
   for (k = 0; k < s->njobs; k++) {
     srv_job *j = s->jobs[k];
     free(j->xd); free(j->fd); free(j->xp); free(j->result); free(j);
