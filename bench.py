@@ -295,12 +295,14 @@ def run_uneven(rk4_steps=3, dopri_steps=5, t_end=0.1, pp_budget_s=90.0):
     return out
 
 
-def run_precision_stress(np_=1_000_000, eps_h=1.0):
+def run_precision_stress(np_=4_000_000, eps_h=1.0, steps=20):
     """The precision-stress configuration: 80^3 jittered lattice, Gaussian kernel with eps_r = eps_h/h
     (h the lattice spacing; eps_h = 1 is the configuration as stated), 16 seeded Fourier modes with
-    amplitudes ~N(0,1)/k^2, 32^3 PU nodes; FP32 evaluation against the all-FP64 path on the same
-    data, max / RMS / pointwise relative error per component, the patches' 1-norm condition
-    estimates beside them, plus the FP64 interpolant against the exact field."""
+    amplitudes ~N(0,1)/k^2, 32^3 PU nodes, np_ uniform particles; the FP32-evaluation path against
+    the all-FP64 path on the same data: max / RMS / pointwise relative error per component of the
+    interpolated field, then (steps > 0) of the positions and fields after `steps` RK4 steps of
+    dt = 5e-4; the patches' 1-norm condition estimates beside them, plus the FP64 interpolant
+    against the exact field."""
     import lagrbf_gb300 as L
     from lagrbf_gb300 import workloads as W
     xd, fd, xp, opts = W.config_precision_3d(np_=np_)
@@ -308,7 +310,8 @@ def run_precision_stress(np_=1_000_000, eps_h=1.0):
     res, kap = {}, None
     for prec in ("fp64", "fp32"):
         log("precision stress: eps_h %g, %s" % (eps_h, prec))
-        c = L.LagRBFCtx(**opts, solve_method=1, eval_precision=prec)
+        c = L.LagRBFCtx(**opts, solve_method=1, eval_precision=prec, advection=steps > 0, advection_scheme=2,
+                        advection_cfl=0.3, dt=DT)
         if prec == "fp64":
             c.set_condition_estimates(True)
         c.fill_data(xd, fd)
@@ -316,19 +319,42 @@ def run_precision_stress(np_=1_000_000, eps_h=1.0):
         c.interpolate_c()
         f = np.zeros((np_, 3))
         c.output(fvals=f)
-        res[prec] = f
+        out = {"f0": f}
         if prec == "fp64":
             kap = c.condition()[1]
+        if steps > 0:
+            ts = time.perf_counter()
+            for k in range(steps):
+                c.advect_resident(k * DT, (k + 1) * DT)
+            c.synchronize()
+            out["seconds"] = time.perf_counter() - ts
+            x = np.zeros((np_, 3)); f = np.zeros((np_, 3)); pid = np.zeros(np_, dtype=np.int64)
+            c.output(coords=x, fvals=f, pidx=pid)
+            out.update(x=x, f=f, alive=pid > 0)
+        res[prec] = out
         del c
-    mx, rms = relerr_stats(res["fp32"], res["fp64"])
+    mx, rms = relerr_stats(res["fp32"]["f0"], res["fp64"]["f0"])
     exact = W.fourier_field(xp, np.random.default_rng(7))
-    ex_mx, ex_rms = relerr_stats(res["fp64"], exact)
-    return {"workload": "80^3 jittered lattice, Gaussian eps_r = %g/h, 16 Fourier modes, 32^3 PU, %d particles"
+    ex_mx, ex_rms = relerr_stats(res["fp64"]["f0"], exact)
+    line = {"workload": "80^3 jittered lattice, Gaussian eps_r = %g/h, 16 Fourier modes, 32^3 PU, %d particles"
                         % (eps_h, np_),
             "kappa1_max": kap["max"], "kappa1_median": kap["median"], "patches": kap["count"],
             "fp32_vs_fp64_max_rel_err": mx, "fp32_vs_fp64_rms_rel_err": rms,
-            "fp32_vs_fp64_pointwise_rel_err": pointwise_relerr(res["fp32"], res["fp64"]),
+            "fp32_vs_fp64_pointwise_rel_err": pointwise_relerr(res["fp32"]["f0"], res["fp64"]["f0"]),
             "fp64_vs_exact_max_rel_err": ex_mx, "fp64_vs_exact_rms_rel_err": ex_rms}
+    if steps > 0:
+        a, b = res["fp32"], res["fp64"]
+        both = a["alive"] & b["alive"]
+        travel = np.abs(b["x"][both] - xp[both]).max()
+        dx = np.abs(a["x"][both] - b["x"][both])
+        fmx, frms = relerr_stats(a["f"][both], b["f"][both])
+        line["rk4_steps"] = {"steps": steps, "dt": DT, "same_alive": bool(np.array_equal(a["alive"], b["alive"])),
+                             "alive_both": int(both.sum()), "pos_max_abs_diff": float(dx.max()),
+                             "pos_rms_abs_diff": float(np.sqrt((dx ** 2).mean())),
+                             "pos_max_diff_rel_to_max_travel": float(dx.max() / travel) if travel > 0 else None,
+                             "field_max_rel_err": fmx, "field_rms_rel_err": frms,
+                             "fp64_seconds": b["seconds"], "fp32_seconds": a["seconds"]}
+    return line
 
 
 def run_trajectory(xd, fd, xp, opts, nsteps=50):
@@ -608,7 +634,7 @@ def main():
     if rank == 0 and world == 1 and args.serve_jobs > 0:
         log("precision stress")
         precision = run_precision_stress()
-        precision["flattened"] = run_precision_stress(np_=250_000, eps_h=0.35)
+        precision["flattened"] = run_precision_stress(np_=250_000, eps_h=0.35, steps=0)
     # ---------------- serving loop: Poisson stream of mixed advection jobs ----------------
     uneven = None
     if rank == 0 and world == 1 and args.uneven:
