@@ -154,3 +154,47 @@ def test_noalloc_accepts_the_largest_mesh():
     assert np.array_equal(cid, t[:, 0] + 1024 * t[:, 1])
     assert start[-1] == len(x) and len(start) == MAX_CELLS + 1
     assert np.array_equal(np.sort(order), np.arange(len(x)))
+
+
+def test_noalloc_records_into_a_stream_capture_and_allocates_nothing():
+    """What the entry point is for: after one call (which resolves the scratch address and loads its
+    kernels), a call changes neither the device memory in use (cudaMemGetInfo) nor torch's
+    allocation, and it can be recorded into the caller's own stream capture (torch.cuda.graph,
+    global capture mode: an allocation or synchronisation inside would invalidate the capture);
+    replaying the graph gives the eager results."""
+    torch = pytest.importorskip("torch")
+    dim, npu, nlat = 3, 6, 18
+    _, xp, _ = _case(dim, npu, nlat, 31)
+    nodes = [npu] * dim
+    ref = _bin_noalloc(torch, dim, nodes, xp)  # warm-up, eager
+    f = _fn()
+    n, ncells = len(xp), (npu - 1) ** dim
+    x = torch.from_numpy(np.ascontiguousarray(xp, dtype=np.float64)).cuda()
+    cid = torch.full((n,), -7, dtype=torch.int32, device="cuda")
+    start = torch.full((ncells + 1,), -7, dtype=torch.int32, device="cuda")
+    order = torch.full((n,), -7, dtype=torch.int32, device="cuda")
+    nodes_c = (ctypes.c_int32 * 3)(*nodes)
+    O_c = (ctypes.c_double * 3)(0.0, 0.0, 0.0)
+    L_c = (ctypes.c_double * 3)(1.0, 1.0, 1.0)
+
+    def call(stream):
+        return f(dim, nodes_c, O_c, L_c, n, x.data_ptr(), cid.data_ptr(), start.data_ptr(), order.data_ptr(),
+                 ctypes.c_void_p(stream))
+
+    torch.cuda.synchronize()
+    free0, alloc0 = torch.cuda.mem_get_info()[0], torch.cuda.memory_allocated()
+    assert call(torch.cuda.current_stream().cuda_stream) == 0
+    torch.cuda.synchronize()
+    assert torch.cuda.mem_get_info()[0] == free0 and torch.cuda.memory_allocated() == alloc0
+    for t, r in zip((cid, start, order), ref):
+        assert np.array_equal(t.cpu().numpy(), r)
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g):
+        assert call(torch.cuda.current_stream().cuda_stream) == 0
+    for t in (cid, start, order):
+        t.fill_(-7)
+    torch.cuda.synchronize()
+    g.replay()
+    torch.cuda.synchronize()
+    for t, r in zip((cid, start, order), ref):
+        assert np.array_equal(t.cpu().numpy(), r)
