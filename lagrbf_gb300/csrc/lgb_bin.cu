@@ -524,6 +524,42 @@ __global__ void k_copy_in(double *__restrict__ dst, const double *__restrict__ s
   }
 }
 
+/* DMSwarmAssignRankFromDMDA's bounding-box check (swarm_utils.c:854-871) of caller coordinates that
+   the device reads directly, fused with the word-for-word comparison against the coordinates already
+   on the device (prev, nullable): flags[0] = some point is outside [O, L], flags[1] = some word
+   differs from prev.  One vote per warp, one atomic per warp that found something. */
+__global__ void k_check_coords(lgb_geom g, int n, const double *x, const double *__restrict__ prev, int *flags)
+{
+  const int dim = g.dim;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  int out = 0, diff = 0;
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n; p += stride) {
+    for (int d = 0; d < dim; d++) {
+      const double v = x[p * dim + d];
+      out |= (v < g.O[d]) | (v > g.L[d]); /* the host check's predicate (NaN passes, as there) */
+      if (prev) diff |= __double_as_longlong(v) != __double_as_longlong(prev[p * dim + d]);
+    }
+  }
+  const unsigned any_out = __ballot_sync(0xffffffffu, out), any_diff = __ballot_sync(0xffffffffu, diff);
+  if ((threadIdx.x & 31) == 0) {
+    if (any_out) atomicOr(&flags[0], 1);
+    if (any_diff) atomicOr(&flags[1], 1);
+  }
+}
+
+extern "C" int lgb_op_check_coords(const lgb_geom *g, int n, const double *x, const double *prev, int *flags, int nsm,
+                                   void *stream)
+{
+  cudaStream_t s = (cudaStream_t)stream;
+  cudaMemsetAsync(flags, 0, 2 * sizeof(int), s);
+  if (n > 0) {
+    const long long need = ((long long)n + 255) / 256, cap = 8LL * (nsm > 0 ? nsm : 1);
+    k_check_coords<<<(int)(need < cap ? need : cap), 256, 0, s>>>(*g, n, x, prev, flags);
+    lgb_count_launch(1);
+  }
+  return (int)cudaGetLastError();
+}
+
 extern "C" int lgb_op_copy_in(double *dst, const double *src, long long words, int nsm, void *stream)
 {
   if (words <= 0) return 0;

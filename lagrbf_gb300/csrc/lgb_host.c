@@ -246,6 +246,8 @@ typedef struct lgb_ctx_s {
   long long *pidd;
   int pidd_cap, pidd_valid;
   int *out_inv, *out_bad;
+  int *chk_flags;  /* flags of the device-side coordinate check of lagrbf_fill_swarm (data) */
+  int xd_valid;    /* d->xd holds the coordinates of the last completed data fill, input order */
   long long out_inv_cap;
   double *hx_d;          /* last filled data coordinates (change detection) */
   int data_filled, points_filled;
@@ -354,7 +356,7 @@ static void destroy_ctx(lgb_ctx *c)
   for (i = 0; i < 2 * NPROF; i++) if (c->ev[i]) cudaEventDestroy(c->ev[i]);
   if (c->hctrl) cudaFreeHost(c->hctrl);
   if (c->stream) cudaStreamDestroy(c->stream);
-  DFREE(c->pidd); DFREE(c->out_inv); DFREE(c->out_bad); DFREE(d->vfield_par);
+  DFREE(c->pidd); DFREE(c->out_inv); DFREE(c->out_bad); DFREE(c->chk_flags); DFREE(d->vfield_par);
   free(c->pid_d); free(c->pid_p); free(c->hx_d);
   free(c);
 }
@@ -835,10 +837,25 @@ static int fill_data(lgb_ctx *c, int n, const double *coords, const double *valu
   lgb_dev *d = &c->d;
   int dim = d->g.dim, F = d->F, err = 0, same_coords;
   int old = d->nd;
+  const int prev_ok = c->xd_valid && n == old && n > 0;
   if (c->shared_from)
     return set_error(LAGRBF_ERR_ARG_WRONGSTATE, "the data swarm is shared from another context (read-only)");
   c->all_ready = 0;
-  TRY(check_box(&d->g, n, coords, (c->hx_d && n == d->nd && n > 0) ? c->hx_d : NULL, &same_coords));
+  c->xd_valid = 0;
+  if (c->out_direct && n > 0) {
+    /* the device reads the caller's array: one pass checks the bounding box and compares the words
+       with the coordinates already on the device (the host pass below only names an offender) */
+    int fl[2] = {0, 0};
+    if (!c->chk_flags) c->chk_flags = (int *)dalloc(2 * sizeof(int), &err);
+    if (err) return set_error(LAGRBF_ERR_MEM, "coordinate check flags allocation failed");
+    OP(lgb_op_check_coords(&d->g, n, coords, prev_ok ? d->xd : NULL, c->chk_flags, d->nsm, c->stream));
+    CU(cudaMemcpyAsync(fl, c->chk_flags, sizeof fl, cudaMemcpyDeviceToHost, c->stream));
+    CU(cudaStreamSynchronize(c->stream));
+    if (fl[0]) TRY(check_box(&d->g, n, coords, NULL, NULL));
+    same_coords = prev_ok && !fl[1];
+  } else {
+    TRY(check_box(&d->g, n, coords, (prev_ok && c->hx_d) ? c->hx_d : NULL, &same_coords));
+  }
   TRY(grow_pids(&c->pid_d, &c->pid_d_cap, old, n));
   if (pidx) memcpy(c->pid_d, pidx, sizeof(int64_t) * (size_t)n);
   else assign_pids(c->pid_d, old, n);
@@ -878,12 +895,16 @@ static int fill_data(lgb_ctx *c, int n, const double *coords, const double *valu
     CU(cudaMemsetAsync(d->setup, 0, sizeof(int) * (size_t)d->g.nnodes, c->stream));
     CU(cudaMemsetAsync(d->solved, 0, sizeof(int) * (size_t)d->g.nnodes, c->stream));
     free(c->hx_d);
-    c->hx_d = (double *)malloc(sizeof(double) * (size_t)(n > 0 ? n : 1) * dim);
-    if (n > 0 && c->hx_d) memcpy(c->hx_d, coords, sizeof(double) * (size_t)n * dim);
+    c->hx_d = NULL;
+    if (!c->out_direct) { /* host copy for the next comparison (the device compares with d->xd) */
+      c->hx_d = (double *)malloc(sizeof(double) * (size_t)(n > 0 ? n : 1) * dim);
+      if (n > 0 && c->hx_d) memcpy(c->hx_d, coords, sizeof(double) * (size_t)n * dim);
+    }
     invalidate_graph(c);
   }
   CU(cudaStreamSynchronize(c->stream));
   c->data_filled = 1;
+  c->xd_valid = 1;
   return 0;
 }
 

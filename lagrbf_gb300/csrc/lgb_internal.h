@@ -234,6 +234,8 @@ int lgb_op_output_rows(int n, const long long *pid, const int *alive, int ngloba
 /* Copies `words` 8-byte words from a host array that the device reads directly (pageable memory
    through the GPU's address translation) into device memory; stream-ordered. */
 int lgb_op_copy_in(double *dst, const double *src, long long words, int nsm, void *stream);
+int lgb_op_check_coords(const lgb_geom *g, int n, const double *x, const double *prev, int *flags, int nsm,
+                        void *stream);
 /* Sets the calling thread's error message (returned by lagrbf_gpu_last_error); returns code. */
 int lgb_set_error_msg(int code, const char *msg);
 long long lgb_launch_count(void);
