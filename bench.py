@@ -62,6 +62,8 @@ def parse():
                     help="setup, reset_coefficients, one re-solve of every patch (kept factors), for ncu")
     ap.add_argument("--serve-jobs", type=int, default=60, help="jobs of the serving leg (0: skip it)")
     ap.add_argument("--uneven", type=int, default=1, help="run the uneven-mixture leg (0: skip it)")
+    ap.add_argument("--uneven-only", default="", help="comma-separated schemes of the uneven leg (rk4, dopri, "
+                    "dopri_per_particle) to run alone, printing that leg's JSON (for profiling it)")
     ap.add_argument("--eval-precision", default="fp32", choices=["fp32", "fp64"],
                     help="evaluation precision of the main context (fp64: the plain path, for profiling it)")
     ap.add_argument("--device-loop", type=int, default=1,
@@ -238,7 +240,8 @@ def run_serving(njobs, workers=8, budget=150e9, sweep=(5.0, 10.0, 20.0, 40.0), s
     return out
 
 
-def run_uneven(rk4_steps=3, dopri_steps=5, t_end=0.1, pp_budget_s=90.0):
+def run_uneven(rk4_steps=3, dopri_steps=5, t_end=0.1, pp_budget_s=90.0, schemes=("rk4", "dopri", "dopri_per_particle"),
+               device_loop=True):
     """The uneven configuration: 1M points (90 % from 8 Gaussians of widths 0.02-0.2, 10 % uniform),
     ABC flow, 8M particles from the same mixture, Wendland C2 on a uniform 160^3 PU mesh (largest
     patch 1,713 points, 2.3M non-empty patches).  Set-up time, then FP32-evaluation RK4 steps at
@@ -252,11 +255,13 @@ def run_uneven(rk4_steps=3, dopri_steps=5, t_end=0.1, pp_budget_s=90.0):
     out = {"workload": "uneven: 1M-point Gaussian mixture + 10% uniform, ABC flow, 160^3 PU, Wendland C2, "
                        "8M particles from the mixture, FP32 evaluation"}
     for scheme, name in ((2, "rk4"), (3, "dopri"), (3, "dopri_per_particle")):
+        if name not in schemes:
+            continue
         pp = name == "dopri_per_particle"
         log("uneven: %s" % name)
         c = L.LagRBFCtx(**opts, advection=True, advection_scheme=scheme, advection_cfl=0.3, solve_method=1,
-                        eval_precision="fp32", dt=DT, petsc_options={"dopri_rtol": 1e-6, "dopri_atol": 1e-9,
-                                                                      "dopri_per_particle": pp})
+                        eval_precision="fp32", dt=DT, device_loop=device_loop,
+                        petsc_options={"dopri_rtol": 1e-6, "dopri_atol": 1e-9, "dopri_per_particle": pp})
         c.synchronize()
         ts = time.perf_counter()
         c.fill_data(xd, fd); c.fill_points(xp); c.interpolate_c(); c.synchronize()
@@ -411,6 +416,9 @@ def main():
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
+    if args.uneven_only:
+        print(json.dumps(run_uneven(schemes=tuple(args.uneven_only.split(",")), device_loop=bool(args.device_loop))))
+        return 0
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
