@@ -586,30 +586,8 @@ __global__ void __launch_bounds__(128) k_build_records(EvalParams P, int force)
   }
 }
 
-/* ---- TMA bulk copies into shared memory, completion tracked by an mbarrier ---- */
+/* shared-memory address of a generic pointer (PTX operands) */
 __device__ __forceinline__ unsigned smem_addr(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
-
-__device__ __forceinline__ void tma_issue(float *dst, const float *src, unsigned bytes, unsigned long long *mbar)
-{
-  const unsigned mb = smem_addr(mbar), d = smem_addr(dst);
-  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mb), "r"(bytes) : "memory");
-  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
-               ::"r"(d), "l"(src), "r"(bytes), "r"(mb) : "memory");
-}
-
-/* Bounded wait for the phase `parity` of an mbarrier; false if it did not complete. */
-__device__ __forceinline__ bool tma_wait(unsigned long long *mbar, unsigned parity)
-{
-  const unsigned mb = smem_addr(mbar);
-  for (int it = 0; it < (1 << 22); ++it) {
-    unsigned done;
-    asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
-                 : "=r"(done) : "r"(mb), "r"(parity) : "memory");
-    if (done) return true;
-  }
-  return false;
-}
 
 /* Round planner (one thread): packs the next records of the block, in neighbour order, into a
    staging buffer of `budget` elements; advances the cursor (o, pp) and returns the elements planned. */
@@ -636,10 +614,10 @@ __device__ __noinline__ int eval_plan(const int *cnt, int budget, int &o, int &p
   return base;
 }
 
-/* STAGE: 0 = gather the records from the coefficient pool each round (any precision, any field
-   range); 1 = stream precomputed FP32 record blocks with TMA bulk copies into two shared-memory
-   buffers (the next round's copy is in flight while the current round computes). */
-template <typename Real, int DIM, int FP, int R, int KER, int STAGE>
+/* The gather evaluation (FP64 path, and FP32 where no record blocks exist): each round the CTA
+   gathers the next records of the block from the coefficient pool into shared memory (any
+   precision, any field range), then every thread evaluates its particles against them. */
+template <typename Real, int DIM, int FP, int R, int KER>
 __global__ void __launch_bounds__(LGB_CHUNK_MAX / R) k_eval(EvalParams P)
 {
   constexpr int NEN = EGeo<DIM>::NEN, NOFF = EGeo<DIM>::NOFF;
@@ -647,9 +625,8 @@ __global__ void __launch_bounds__(LGB_CHUNK_MAX / R) k_eval(EvalParams P)
   extern __shared__ __align__(16) unsigned char smem_raw[];
   Real *sm = reinterpret_cast<Real *>(smem_raw);
   __shared__ int s_cnt[27], s_first[27], s_node[8], s_setup[8];
-  __shared__ int s_seg_o[2][27], s_seg_p0[2][27], s_seg_n[2][27], s_seg_base[2][27], s_nseg[2];
+  __shared__ int s_seg_o[1][27], s_seg_p0[1][27], s_seg_n[1][27], s_seg_base[1][27], s_nseg[1];
   __shared__ long long s_pre[28];
-  __shared__ __align__(8) unsigned long long s_mbar[2];
   __shared__ int s_o, s_pp, s_cell, s_pbeg, s_pn, s_blk, s_wsum;
   const lgb_geom &g = P.g;
   const int tid = threadIdx.x;
@@ -721,9 +698,9 @@ __global__ void __launch_bounds__(LGB_CHUNK_MAX / R) k_eval(EvalParams P)
 #pragma unroll
       for (int f = 0; f < FP; f++) acc[r][k][f] = Real(0);
 
-  /* shared memory: [staging buffer 0 | staging buffer 1 (TMA only)] [FP32 running sums: one block of
-     R*NEN*FP (+1 pad, odd stride: no bank conflicts) floats per thread] */
-  const int nbuf = (STAGE == 1) ? 2 : 1;
+  /* shared memory: [staging buffer] [FP32 running sums: one block of R*NEN*FP (+1 pad, odd stride:
+     no bank conflicts) floats per thread] */
+  const int nbuf = 1;
   constexpr int RUNB = R * NEN * FP + 1;
   float *run = reinterpret_cast<float *>(sm + (size_t)nbuf * P.budget) + (size_t)tid * RUNB;
   const int rstride = 0;
@@ -735,71 +712,28 @@ __global__ void __launch_bounds__(LGB_CHUNK_MAX / R) k_eval(EvalParams P)
   const Real ga = (Real)(-(g.eps_r * g.eps_r) * 1.4426950408889634);
   const int kernel = g.kernel;
 
-  if constexpr (STAGE == 1) {
+  for (;;) {
     if (tid == 0) {
-      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&s_mbar[0])) : "memory");
-      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&s_mbar[1])) : "memory");
-      asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-      const int o0 = s_o, pp0 = s_pp;
       int o = s_o, pp = s_pp;
-      const int n = eval_plan<Real, DIM, FP>(s_cnt, P.budget, o, pp, s_seg_o[0], s_seg_p0[0], s_seg_n[0], s_seg_base[0],
-                                             &s_nseg[0]);
+      eval_plan<Real, DIM, FP>(s_cnt, P.budget, o, pp, s_seg_o[0], s_seg_p0[0], s_seg_n[0], s_seg_base[0], &s_nseg[0]);
       s_o = o; s_pp = pp;
-      if (n > 0) {
-        const float *src = P.rec32 + P.rec_off[cell] + s_pre[o0] + (long long)pp0 * erec<float>(epopc(einv_mask(DIM, o0)), FP);
-        tma_issue(reinterpret_cast<float *>(sm), src, (unsigned)n * 4u, &s_mbar[0]);
-      }
     }
     __syncthreads();
-    for (int r = 0;; r++) {
-      const int b = r & 1;
-      const int nseg = s_nseg[b];
-      if (nseg == 0) break;
-      if (tid == 0) {
-        const int o0 = s_o, pp0 = s_pp;
-        int o = s_o, pp = s_pp;
-        const int n = eval_plan<Real, DIM, FP>(s_cnt, P.budget, o, pp, s_seg_o[b ^ 1], s_seg_p0[b ^ 1], s_seg_n[b ^ 1],
-                                               s_seg_base[b ^ 1], &s_nseg[b ^ 1]);
-        s_o = o; s_pp = pp;
-        if (n > 0) {
-          const float *src = P.rec32 + P.rec_off[cell] + s_pre[o0] + (long long)pp0 * erec<float>(epopc(einv_mask(DIM, o0)), FP);
-          tma_issue(reinterpret_cast<float *>(sm) + (size_t)(b ^ 1) * P.budget, src, (unsigned)n * 4u, &s_mbar[b ^ 1]);
-        }
-      }
-      const bool ok = tma_wait(&s_mbar[b], (unsigned)((r >> 1) & 1));
-      if (!ok && tid == 0) atomicExch(&P.ctrl->eval_error, 1);
-      if (ok && warp_active) {
-        const Real *buf = sm + (size_t)b * P.budget;
-        for (int sgi = 0; sgi < nseg; sgi++)
-          eval_dispatch<Real, DIM, FP, R, KER>(s_seg_o[b][sgi], buf + s_seg_base[b][sgi], s_seg_n[b][sgi], px, acc,
-                                                eps, ga, kernel, run, rstride);
-      }
-      __syncthreads();
+    const int nseg = s_nseg[0];
+    if (nseg == 0) break;
+    for (int sgi = 0; sgi < nseg; sgi++) {
+      const int o = s_seg_o[0][sgi], p0 = s_seg_p0[0][sgi], n = s_seg_n[0][sgi];
+      const int S = erec<Real>(epopc(einv_mask(DIM, o)), FP);
+      Real *rbase = sm + s_seg_base[0][sgi];
+      for (int p = tid; p < n; p += EVAL_T)
+        write_record<Real, DIM, FP>(P, o, p0 + p, s_first[o] + p0 + p, s_node, s_setup, rbase + (size_t)p * S);
     }
-  } else {
-    for (;;) {
-      if (tid == 0) {
-        int o = s_o, pp = s_pp;
-        eval_plan<Real, DIM, FP>(s_cnt, P.budget, o, pp, s_seg_o[0], s_seg_p0[0], s_seg_n[0], s_seg_base[0], &s_nseg[0]);
-        s_o = o; s_pp = pp;
-      }
-      __syncthreads();
-      const int nseg = s_nseg[0];
-      if (nseg == 0) break;
-      for (int sgi = 0; sgi < nseg; sgi++) {
-        const int o = s_seg_o[0][sgi], p0 = s_seg_p0[0][sgi], n = s_seg_n[0][sgi];
-        const int S = erec<Real>(epopc(einv_mask(DIM, o)), FP);
-        Real *rbase = sm + s_seg_base[0][sgi];
-        for (int p = tid; p < n; p += EVAL_T)
-          write_record<Real, DIM, FP>(P, o, p0 + p, s_first[o] + p0 + p, s_node, s_setup, rbase + (size_t)p * S);
-      }
-      __syncthreads();
-      if (warp_active)
-        for (int sgi = 0; sgi < nseg; sgi++)
-          eval_dispatch<Real, DIM, FP, R, KER>(s_seg_o[0][sgi], sm + s_seg_base[0][sgi], s_seg_n[0][sgi], px, acc,
-                                                eps, ga, kernel, run, rstride);
-      __syncthreads();
-    }
+    __syncthreads();
+    if (warp_active)
+      for (int sgi = 0; sgi < nseg; sgi++)
+        eval_dispatch<Real, DIM, FP, R, KER>(s_seg_o[0][sgi], sm + s_seg_base[0][sgi], s_seg_n[0][sgi], px, acc,
+                                              eps, ga, kernel, run, rstride);
+    __syncthreads();
   }
 
   /* epilogue: PU weights and the weighted sum */

@@ -4,27 +4,27 @@
 #include "lgb_evalrec.cuh"
 #include <stdlib.h>
 
-template <int DIM, int FP, int KER, int STAGE, int R>
+template <int DIM, int FP, int KER, int R>
 static int launch32r(const EvalParams &P, int grid, cudaStream_t s)
 {
   static bool attr = false;
-  const int nbuf = (STAGE == 1) ? 2 : 1;
+  const int nbuf = 1;
   /* staging buffer(s) + per-thread running sums of the R*NEN*FP per-patch partial sums */
   size_t smem = ((size_t)nbuf * P.budget + (size_t)(R * (1 << DIM) * FP + 1) * (P.chunk_cap / R)) * sizeof(float);
   if (!attr) {
     size_t smax = ((size_t)nbuf * P.budget + (size_t)(R * (1 << DIM) * FP + 1) * (LGB_CHUNK_MAX / R)) * sizeof(float);
-    cudaFuncSetAttribute(k_eval<float, DIM, FP, R, KER, STAGE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smax);
+    cudaFuncSetAttribute(k_eval<float, DIM, FP, R, KER>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smax);
     attr = true;
   }
-  k_eval<float, DIM, FP, R, KER, STAGE><<<grid, P.chunk_cap / R, smem, s>>>(P);
+  k_eval<float, DIM, FP, R, KER><<<grid, P.chunk_cap / R, smem, s>>>(P);
   return (int)cudaGetLastError();
 }
 
 /* Two particles per thread (four per thread measured slower: fewer active lanes per work unit). */
-template <int DIM, int FP, int KER, int STAGE>
+template <int DIM, int FP, int KER>
 static int launch32(const EvalParams &P, int grid, cudaStream_t s)
 {
-  return launch32r<DIM, FP, KER, STAGE, 2>(P, grid, s);
+  return launch32r<DIM, FP, KER, 2>(P, grid, s);
 }
 
 /* The record-streamed kernel: EVR_NB stages of P.budget floats, then the PU-weight pairs. */
@@ -52,10 +52,10 @@ static int launch32_fp(const EvalParams &P, int fp, int stage, int grid, cudaStr
 {
   if (stage == 1) return launch_rec<DIM, KER>(P, grid, s); /* records hold the dim velocity fields */
   switch (fp) {
-  case 1: return launch32<DIM, 1, KER, 0>(P, grid, s);
-  case 2: return launch32<DIM, 2, KER, 0>(P, grid, s);
-  case 3: return launch32<DIM, 3, KER, 0>(P, grid, s);
-  default: return launch32<DIM, 4, KER, 0>(P, grid, s);
+  case 1: return launch32<DIM, 1, KER>(P, grid, s);
+  case 2: return launch32<DIM, 2, KER>(P, grid, s);
+  case 3: return launch32<DIM, 3, KER>(P, grid, s);
+  default: return launch32<DIM, 4, KER>(P, grid, s);
   }
 }
 

@@ -11,7 +11,8 @@ extern "C" int lgb_eval32_launch_2d(const EvalParams *P, int fp, int ker, int st
 extern "C" int lgb_build_records_3d(const EvalParams *P, int force, int grid, void *stream);
 extern "C" int lgb_build_records_2d(const EvalParams *P, int force, int grid, void *stream);
 
-/* Staging budgets (elements): FP32 gather 30 KB, FP32 record stream 4 stages x 4 KB, FP64 48 KB. */
+/* Staging budgets (elements): FP32 gather 30 KB, FP32 record stream per stage from the measured
+   table (lgb_eval_tune.h: stage count and size), FP64 48 KB. */
 #define BUDGET32 7680
 #include "lgb_eval_tune.h"
 #define BUDGET32_TMA LGB_TMA_BUDGET_TUNED /* floats per staging round of the record kernel */
@@ -25,11 +26,11 @@ static int launch64(const EvalParams &P, int grid, cudaStream_t s)
   static bool attr = false;
   size_t smem = (size_t)P.budget * sizeof(double);
   if (!attr) {
-    cudaFuncSetAttribute(k_eval<double, DIM, FP, 1, KER_GENERIC, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaFuncSetAttribute(k_eval<double, DIM, FP, 1, KER_GENERIC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)smem);
     attr = true;
   }
-  k_eval<double, DIM, FP, 1, KER_GENERIC, 0><<<grid, P.chunk_cap, smem, s>>>(P);
+  k_eval<double, DIM, FP, 1, KER_GENERIC><<<grid, P.chunk_cap, smem, s>>>(P);
   return (int)cudaGetLastError();
 }
 
