@@ -1,6 +1,7 @@
 """Serving loop on the GPU: a mix of jobs (three datasets, two kept resident by id and reused,
-all four RK schemes, FP32 and FP64 evaluation) run concurrently by four workers gives, job by job,
-the same particle positions bit for bit as each job run alone; latency statistics are reported."""
+all four RK schemes, FP32 and FP64 evaluation, two CFL factors) run concurrently by four workers
+(owner and sharing contexts, sharing contexts reused between jobs) gives, job by job, the same
+particle positions bit for bit as each job run alone; latency statistics are reported."""
 import numpy as np
 import pytest
 
@@ -30,7 +31,8 @@ def _jobs():
         np_ = int(rng.integers(500, 3000))
         xp = 0.1 + 0.8 * rng.uniform(0, 1, (np_, 3))
         job = dict(npartitions=[npu] * 3, particles=xp, dt=2e-3, nsteps=int(rng.integers(2, 5)), scheme=k % 4,
-                   fp32=bool(k % 2), dataset_id=(which + 1) if which < 2 else 0)
+                   fp32=bool(k % 2), dataset_id=(which + 1) if which < 2 else 0,
+                   cfl=0.3 if k % 3 else 0.004)  # 0.004: the CFL step (~1e-3) limits the internal step
         first = which == 2 or k < 2
         if first:
             job.update(data_coords=xd, data_values=fd)
