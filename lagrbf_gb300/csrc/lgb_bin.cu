@@ -390,17 +390,27 @@ __global__ void k_mark(lgb_geom g, int np, const int *__restrict__ cell, const i
   }
 }
 
-/* Queued patches into the work-list region of their size class (cls_off); nwork counts them all. */
-__global__ void k_compact(int nnodes, int *__restrict__ need, const int *__restrict__ pm,
-                          const int *__restrict__ cls_off, int *__restrict__ work, lgb_ctrl *ctrl)
+/* Queued patches into the work-list region of their size class (cls_off); nwork counts them all.
+   The cells around a queued patch node (up to 2^dim) are marked for a record rebuild. */
+__global__ void k_compact(lgb_geom g, int *__restrict__ need, const int *__restrict__ pm,
+                          const int *__restrict__ cls_off, int *__restrict__ work, lgb_ctrl *ctrl,
+                          unsigned char *__restrict__ cdirty)
 {
   int node = blockIdx.x * blockDim.x + threadIdx.x;
-  if (node >= nnodes) return;
+  if (node >= g.nnodes) return;
   if (need[node]) {
     need[node] = 0;
     const int c = lgb_patch_class(pm[node]);
     work[cls_off[c] + atomicAdd(&ctrl->nwork_c[c], 1)] = node;
     atomicAdd(&ctrl->nwork, 1);
+    const int i = node % g.n[0], j = (node / g.n[0]) % g.n[1], k = node / (g.n[0] * g.n[1]);
+    for (int dk = (g.dim == 3) ? -1 : 0; dk <= 0; dk++)
+      for (int dj = -1; dj <= 0; dj++)
+        for (int di = -1; di <= 0; di++) {
+          const int a = i + di, b = j + dj, e = k + dk;
+          if (a < 0 || b < 0 || e < 0 || a >= g.nc[0] || b >= g.nc[1] || e >= g.nc[2]) continue;
+          cdirty[a + b * g.nc[0] + e * g.nc[0] * g.nc[1]] = 1;
+        }
   }
 }
 
@@ -424,8 +434,8 @@ extern "C" int lgb_op_mark_patches(lgb_dev *d, void *stream)
     k_mark<<<lgb_cdiv(d->np, 256), 256, 0, s>>>(d->g, d->np, d->cell_p, d->alive, d->setup, d->solved, d->need);
     lgb_count_launch(1);
   }
-  k_compact<<<lgb_cdiv(d->g.nnodes, 256), 256, 0, s>>>(d->g.nnodes, d->need, d->pm, d->cls_off_dev, d->work,
-                                                        d->ctrl);
+  k_compact<<<lgb_cdiv(d->g.nnodes, 256), 256, 0, s>>>(d->g, d->need, d->pm, d->cls_off_dev, d->work, d->ctrl,
+                                                        d->cdirty);
   lgb_count_launch(1);
   LGB_CHECK_LAUNCH();
   return 0;

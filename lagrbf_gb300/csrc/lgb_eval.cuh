@@ -55,6 +55,7 @@ struct EvalParams {
   const long long *rec_off;
   int poll_limit;         /* polls of a bounded mbarrier wait before it gives up          */
   int withhold_copies;    /* test hook: arm the staging barriers but issue no copy         */
+  unsigned char *cdirty;  /* cells whose record blocks must be rebuilt (set by the work-list compaction) */
 };
 
 enum { KER_GENERIC = 0, KER_C2 = 1, KER_GAUSS = 2 };

@@ -129,6 +129,7 @@ extern "C" int lgb_op_build_records(lgb_dev *d, int force, void *stream)
   P.ctrl = d->ctrl;
   P.rec32 = d->rec32;
   P.rec_off = d->rec_off;
+  P.cdirty = d->cdirty;
   int grid = d->g.ncells < 8 * d->nsm ? d->g.ncells : 8 * d->nsm;
   int rc = (d->g.dim == 3) ? lgb_build_records_3d(&P, force, grid, stream) : lgb_build_records_2d(&P, force, grid, stream);
   lgb_count_launch(1);

@@ -243,9 +243,11 @@ __device__ __forceinline__ void evr_piece(int vs, int flags, const float *rec, i
   }
 }
 
-/* Builds the record blocks of every cell into P.rec32 at P.rec_off[cell] (FP fields from field 0).
-   Runs only when `force` or when the preceding factorisation launch set up or solved at least one
-   patch (device-side count), so the launch can sit in the captured step graph. */
+/* Builds the record blocks into P.rec32 at P.rec_off[cell] (FP fields from field 0): every cell when
+   `force`, else the cells marked in P.cdirty (the cells around the patches the preceding set-up /
+   solve launch processed: their records carry those patches' coefficients), and only when that
+   launch processed at least one patch (device-side count), so the launch can sit in the captured
+   step graph.  Marks are cleared as the cells are rebuilt. */
 template <int DIM, int FP>
 __global__ void __launch_bounds__(128) k_build_records2(EvalParams P, int force)
 {
@@ -255,6 +257,7 @@ __global__ void __launch_bounds__(128) k_build_records2(EvalParams P, int force)
   const lgb_geom &g = P.g;
   const double eps = evr_scale(g);
   for (int cell = blockIdx.x; cell < g.ncells; cell += gridDim.x) {
+    if (!force && !P.cdirty[cell]) continue; /* the same for the whole block */
     cell_block<DIM>(P, cell, s_cnt, s_first, s_node, s_setup);
     __syncthreads();
     int ci, cj, cl;
@@ -291,6 +294,7 @@ __global__ void __launch_bounds__(128) k_build_records2(EvalParams P, int force)
       dst += (size_t)s_cnt[o] * S;
     }
     __syncthreads();
+    if (threadIdx.x == 0) P.cdirty[cell] = 0;
   }
 }
 

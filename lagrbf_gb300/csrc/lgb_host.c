@@ -352,7 +352,7 @@ static void destroy_ctx(lgb_ctx *c)
   DFREE(d->need); DFREE(d->work); DFREE(d->status); DFREE(d->coff); DFREE(d->foff); DFREE(d->c64); DFREE(d->kappa);
   DFREE(d->c32); DFREE(d->fac); DFREE(d->ws); DFREE(d->pcount); DFREE(d->pstart); DFREE(d->pfill);
   DFREE(d->chunk_start); DFREE(d->scan_tmp); DFREE(d->scan_tmp64); DFREE(d->ctrl);
-  DFREE(d->rec32); DFREE(d->rec_off); DFREE(d->bkey_buf); DFREE(d->cls_off_dev);
+  DFREE(d->rec32); DFREE(d->rec_off); DFREE(d->bkey_buf); DFREE(d->cls_off_dev); DFREE(d->cdirty);
   for (i = 0; i < 2 * NPROF; i++) if (c->ev[i]) cudaEventDestroy(c->ev[i]);
   if (c->hctrl) cudaFreeHost(c->hctrl);
   if (c->stream) cudaStreamDestroy(c->stream);
@@ -574,6 +574,7 @@ static int create_ctx(lgb_ctx **out)
   d->pstart = (int *)dalloc(sizeof(int) * (size_t)(nc + 1), &err);
   d->pfill = (int *)dalloc(sizeof(int) * (size_t)(nc + 1), &err);
   d->chunk_start = (int *)dalloc(sizeof(int) * (size_t)(nc + 1), &err);
+  d->cdirty = (unsigned char *)dalloc((size_t)nc, &err);
   d->scan_tmp = (int *)dalloc(sizeof(int) * 4096, &err);
   d->scan_tmp64 = (long long *)dalloc(sizeof(long long) * 4096, &err);
   d->ctrl = (lgb_ctrl *)dalloc(sizeof(lgb_ctrl), &err);
@@ -593,6 +594,7 @@ static int create_ctx(lgb_ctx **out)
   cudaMemsetAsync(d->cstart, 0, sizeof(int) * (size_t)(nc + 1), c->stream);
   cudaMemsetAsync(d->pstart, 0, sizeof(int) * (size_t)(nc + 1), c->stream);
   cudaMemsetAsync(d->chunk_start, 0, sizeof(int) * (size_t)(nc + 1), c->stream);
+  cudaMemsetAsync(d->cdirty, 0, (size_t)nc, c->stream);
   memset(c->hctrl, 0, sizeof(lgb_ctrl));
   c->hctrl->dt_adv = c->dt0;
   c->hctrl->cfl_fac = c->cfl_fac;
@@ -891,9 +893,12 @@ static int fill_data(lgb_ctx *c, int n, const double *coords, const double *valu
     OP(lgb_op_data_arrange(d, c->stream));
     TRY(ensure_pools(c));
     TRY(ensure_records(c));
-    /* membership changed: every patch must be set up again */
+    /* membership changed: every patch must be set up again, and every cell's record block is
+       rewritten now (no patch set up: zero coefficients), so that cells whose patches stay
+       untouched hold no records of the previous data */
     CU(cudaMemsetAsync(d->setup, 0, sizeof(int) * (size_t)d->g.nnodes, c->stream));
     CU(cudaMemsetAsync(d->solved, 0, sizeof(int) * (size_t)d->g.nnodes, c->stream));
+    OP(lgb_op_build_records(d, 1, c->stream));
     free(c->hx_d);
     c->hx_d = NULL;
     if (!c->out_direct) { /* host copy for the next comparison (the device compares with d->xd) */

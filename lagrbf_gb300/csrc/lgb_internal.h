@@ -171,6 +171,7 @@ typedef struct {
   /* precomputed FP32 record blocks streamed by TMA (NULL: gather staging) */
   float *rec32;
   long long *rec_off;
+  unsigned char *cdirty; /* [ncells] cells whose record blocks the next rebuild must write */
   long long *bkey_buf; /* device storage of g.bkey (cell-face keys) */
   long long rec_cap;
   int rec_fp;          /* fields per record (= dim) */

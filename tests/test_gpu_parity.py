@@ -489,6 +489,35 @@ def test_uneven_mixture_matches_oracle(scheme):
         assert abs(c.stats()["dt"] - o.dt()) <= 1e-9 * abs(o.dt())
 
 
+@pytest.mark.parametrize("solve_method", [1, 2])
+def test_fp32_records_follow_lazy_setup(solve_method):
+    """The FP32 path's record blocks are rebuilt only for the cells around the patches each set-up /
+    solve launch processed.  On the uneven mixture particles keep entering cells whose patches get
+    set up during the run, and the data is refilled between intervals (same coordinates; A_KSP keeps
+    the set-ups, A_KSP_ASMB rebuilds them): FP32 positions and fields stay within the FP32 error of
+    the FP64 path, which reads no records."""
+    xd, fd, xp, opts = W.config_uneven_3d(nd=10000, npu=24, np_=15000, seed=5)
+    adv = dict(advection=True, advection_scheme=2, advection_cfl=0.3, solve_method=solve_method)
+    out = {}
+    for prec in ("fp64", "fp32"):
+        c = gpu_ctx(opts, **adv, eval_precision=prec)
+        c.fill_points(xp)
+        t, dt = 0.0, 5e-3
+        setups = []
+        for _ in range(3):
+            c.fill_data(xd, fd); c.interpolate_c()
+            setups.append(c.stats()["npatch_setup"])
+            c.advect_interpolate_c(t, t + dt)
+            t += dt
+        out[prec] = gpu_output(c, len(xp), 3), setups
+    (x64, f64, p64), s64 = out["fp64"]
+    (x32, f32, p32), s32 = out["fp32"]
+    assert s64 == s32
+    assert np.array_equal(p64, p32)
+    assert np.abs(x32 - x64).max() <= 1e-6
+    assert relerr(f32, f64) <= 1e-5
+
+
 def test_uneven_mixture_per_particle_dopri_matches_oracle():
     """Per-particle Dormand-Prince (option dopri_per_particle) on the uneven mixture, where particles
     in dense clusters and in sparse cells need very different steps: the GPU and the oracle take the
