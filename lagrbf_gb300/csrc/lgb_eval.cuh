@@ -8,6 +8,10 @@
  *   v_f(x_p) = sum_{k in corners(cell p)} w_k(x_p) * sum_{j in patch k} phi(|x_p - x_j|, eps_r) X_k[j, f]
  *   w_k(x)   = phiW(|x - c_k|, eps_w) / sum_{all nodes n} phiW(|x - c_n|, eps_w)     (Wendland C2)
  *
+ * This file holds the gather evaluation (the FP64 path, and FP32 where no record blocks exist) and
+ * the pieces both evaluations share; the FP32 evaluation from TMA-streamed record blocks, the hot
+ * kernel of the FP32 path, is k_eval_rec in lgb_evalrec.cuh.
+ *
  * GB300 design.  Particles are binned by cell every stage; one CTA evaluates one work unit of up to
  * chunk_cap particles of one cell.  The CTA walks the 3^dim neighbour cells of its cell in the
  * reference's neighbour order, staging for each neighbour cell a record per data point
@@ -51,7 +55,7 @@ struct EvalParams {
   lgb_ctrl *ctrl;
   int budget;             /* staging budget, elements of the compute type (per buffer) */
   int chunk_cap;          /* particles per work unit (blockDim.x * R)     */
-  float *rec32;           /* precomputed FP32 record blocks (TMA staging)  */
+  float *rec32;           /* precomputed FP32 record blocks (streamed by k_eval_rec) */
   const long long *rec_off;
   int poll_limit;         /* polls of a bounded mbarrier wait before it gives up          */
   int withhold_copies;    /* test hook: arm the staging barriers but issue no copy         */

@@ -1,6 +1,6 @@
 /*
  * lgb_internal.h -- state shared by the C host layer (lgb_host.c) and the CUDA operations
- * (lgb_bin.cu, lgb_eval.cu, lgb_factor.cu, lgb_step.cu).  Plain C: device memory appears as
+ * (lgb_bin.cu, lgb_eval32_{2,3}d.cu, lgb_eval64.cu, lgb_factor.cu, lgb_step.cu, lgb_noalloc.cu).  Plain C: device memory appears as
  * typed pointers, streams as void*.
  *
  * HBM layout of one context (all arrays device-resident for the lifetime of the dataset):
